@@ -1,0 +1,133 @@
+/*
+ * oocdag_gb300 -- GB300 (sm_103a) out-of-core left-looking tiled Cholesky.
+ *
+ * C-ABI of the library.  Plain pointers and sizes only; every entry point returns an
+ * int status (OOC_OK = 0, negative = error) unless stated otherwise.  Matrices are
+ * column-major; only the lower triangle is read and written ('L').
+ *
+ * Each entry point names the reference interface it replaces (paths relative to the
+ * efdazedo/oocdag project).
+ */
+#ifndef OOCDAG_GB300_H
+#define OOCDAG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+/* -1 .. -99: the k-th argument is invalid (LAPACK convention, -k).                 */
+#define OOC_OK 0
+#define OOC_ERR_NOMEM (-101)     /* device or pinned-host allocation failed          */
+#define OOC_ERR_CUDA (-102)      /* a CUDA call failed; see ooc_last_error_string()  */
+#define OOC_ERR_TIMEOUT (-103)   /* a bounded host wait on the device ran out        */
+#define OOC_ERR_BUDGET (-104)    /* device budget too small for one panel column     */
+#define OOC_ERR_INTERNAL (-105)  /* internal limit exceeded                          */
+#define OOC_ERR_NODEVICE (-106)  /* no CUDA device / device index out of range       */
+#define OOC_ERR_UNSUPPORTED (-107)
+
+typedef struct ooc_handle ooc_handle;
+
+/* Statistics of one factorization (filled when the caller passes a non-NULL pointer). */
+typedef struct ooc_stats {
+  double seconds;          /* factorization wall time (allocation excluded, as
+                              oocdag.cpp:41,51,90 measures it)                       */
+  double flops;            /* n^3/3                                                  */
+  double h2d_bytes;        /* host -> device bytes scheduled                         */
+  double d2h_bytes;        /* device -> host bytes scheduled                         */
+  int npanels;             /* left-looking panels (1 = in-core)                     */
+  int info;                /* LAPACK info                                           */
+  int64_t kernel_launches; /* kernels launched by the library for this call         */
+  /* Per-kernel device time, recorded with CUDA events on the compute stream when
+     OOC_OPT_PROFILE is set (0 otherwise).                                          */
+  double update_ms;        /* panel-update (syrk+gemm) kernels                       */
+  int64_t update_launches;
+  double update_flops;     /* algorithmic flops of those launches                    */
+  double factor_ms;        /* diagonal factor + column solve                         */
+} ooc_stats;
+
+/* Options (ooc_set_option). */
+enum {
+  OOC_OPT_X_BUFFERS = 1,   /* 1 = the reference's single X buffer, 2 = double-buffered
+                              X (default 2; copy of column k+1 overlaps update k)    */
+  OOC_OPT_TIMEOUT_MS = 2,  /* bound on every host wait for the device (default 6 h)  */
+  OOC_OPT_PROFILE = 3,     /* 1 = time kernels with CUDA events into ooc_stats       */
+  OOC_OPT_PIN_HOST = 4,    /* 1 = page-lock a pageable host matrix for the call
+                              (cudaHostRegister; default 1)                          */
+  OOC_OPT_REF_SCHEDULE = 5 /* 1 = panel widths exactly as oocdag.cpp:478-492 with one
+                              X buffer counted (default 0: two X buffers counted)     */
+};
+
+/* Handles: one per thread of control; reentrant across handles. */
+int ooc_create(ooc_handle** h, int device);
+int ooc_destroy(ooc_handle* h);
+int ooc_set_option(ooc_handle* h, int key, int64_t value);
+int ooc_get_option(ooc_handle* h, int key, int64_t* value);
+const char* ooc_last_error_string(void);
+/* LAPACK info of the last factorization run on the handle. */
+int ooc_last_info(ooc_handle* h);
+/* The handle's CUDA streams (which: 0 = compute, 1 = host-to-device copies,
+ * 2 = device-to-host copies), as a cudaStream_t, so that a caller can order its own
+ * work or timing events against the library's.                                     */
+int ooc_get_stream(ooc_handle* h, int which, void** stream);
+
+/* Lower Cholesky A = L L^T in place, out of core.
+ * Replaces: double Cholesky(Quark*, double *A, int N, int NB, int LDA, size_t memsize)
+ *           (oocdag.cpp:18-112) together with its task generators A2Y/A2X/ooc_syrk/
+ *           ooc_incore (oocquark.cpp:253-421, prototypes oocdag.h:119-123).
+ * A: host memory (pageable or pinned; streamed through a device budget of dev_budget
+ *    bytes) or device memory (factored in place, in core).  Upper triangle untouched.
+ * *info: 0, or k > 0 if the leading minor of order k is not positive definite.      */
+int ooc_dpotrf_L(ooc_handle* h, double* A, int64_t n, int64_t lda, int nb, size_t dev_budget,
+                 int* info, ooc_stats* stats);
+
+/* Drop-in for the reference driver entry (oocdag.cpp:18): same argument order, the
+ * QUARK context replaced by an ooc_handle (NULL = a per-process handle on the current
+ * device).  Returns the factorization time in seconds, or a negative status code.  */
+double Cholesky(void* handle, double* A, int N, int NB, int LDA, size_t memsize);
+
+/* ScaLAPACK-style entry (pdpotrf_ argument order) on a 1 x 1 process grid, as the
+ * reference's test matrices are described (desc layout DTYPE_,CTXT_,M_,N_,MB_,NB_,
+ * RSRC_,CSRC_,LLD_, LIN/pdpotrrv.f:118-120).  Only uplo = 'L'.  The tile size is
+ * desca[5] (NB_), the leading dimension desca[8] (LLD_).  The device budget is the
+ * OOC_DEVICE_BUDGET_MB environment variable, else 3/4 of free device memory.      */
+void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, const int* ja,
+                  const int* desca, int* info);
+
+/* Panel plan of the left-looking loop: writes (jb, Ym, Yn) triples for an n x n matrix,
+ * tile nb and a budget of memBlock tiles, counting nx X buffers (nx = 1 reproduces
+ * find_Yn and the panel loop of oocdag.cpp:59-66,478-492).  Host only, no GPU.
+ * Returns the number of panels, OOC_ERR_BUDGET, or -5 if cap triples do not suffice. */
+int ooc_panel_plan(int64_t n, int nb, int64_t memBlock, int nx, int* out, int cap);
+
+/* ---- test matrices (the reference's generator, and the uniform generator) ------ */
+/* pdmatgen('Symm','Diag') on a 1 x 1 grid (LIN/pdmatgen.f, called at oocdag.cpp:298-302):
+ * A(i,j) = 1 - 2 u[min(i,j) n + max(i,j)], A(i,i) = |A(i,i)| + n, u from the 31-bit LCG
+ * x <- 1103515245 x + 12345 mod 2^31 started at x0 = 1103515245 seed + 12345.
+ * A: host or device.                                                               */
+int ooc_dmatgen_pdmatgen(ooc_handle* h, double* A, int64_t n, int64_t lda, int seed);
+/* A = (R + R^T)/2 + alpha I, R(i,j) = u - 1/2 with u the top 53 bits of SplitMix64
+ * output number i + j n (state started at mix(seed)).  Exact in binary64.  No
+ * reference counterpart (the uniform test matrix of the benchmark configurations).  */
+int ooc_dmatgen_uniform(ooc_handle* h, double* A, int64_t n, int64_t lda, uint64_t seed,
+                        double alpha);
+
+/* Scaled residual ||A - L L^T||_F / (n eps ||A||_F), eps = 2^-53, with A regenerated
+ * from its seed tile by tile (kind 0: uniform with alpha; kind 1: pdmatgen with seed)
+ * as LIN/pdlaschk.f:238-250 regenerates it.  L: lower triangle, host or device.     */
+int ooc_dresidual(ooc_handle* h, const double* L, int64_t n, int64_t lda, int kind, uint64_t seed,
+                  double alpha, double* resid);
+
+/* FP64 DMMA issue-rate probe: runs an MMA-only loop on every SM for about `ms`
+ * milliseconds and returns the achieved FP64 tensor rate in TFLOP/s (the FP64 peak
+ * used as the roofline denominator).  No reference counterpart.                     */
+int ooc_fp64_peak_probe(ooc_handle* h, double ms, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OOCDAG_GB300_H */

@@ -1,0 +1,92 @@
+// Shared definitions for the GB300 out-of-core Cholesky library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/oocdag_gb300.h"
+
+typedef int64_t i64;
+
+// Packed panel layout: the lower trapezoid of a panel of Ym tile rows, column of tiles
+// after column of tiles, each tile nb x nb with leading dimension nb.  Tile (i, j),
+// i >= j, starts at tile index i + j*Ym - j*(j+1)/2 (the layout of oocquark.cpp:256).
+__host__ __device__ inline i64 packed_tile_index(int i, int j, int Ym) {
+  return (i64)i + (i64)j * Ym - ((i64)j * (j + 1)) / 2;
+}
+
+// Addressing of a grid of nb x nb tiles.  Either packed (as above, ld = nb) or strided
+// (a column-major matrix with leading dimension ld; tile (i, j) starts at row i*nb,
+// column j*nb).
+struct TileMap {
+  double* base;
+  i64 ld;      // leading dimension of every tile
+  int packed;  // 1: packed trapezoid, 0: strided
+  int Ym;      // packed: tile rows of the panel
+  int nb;
+};
+
+__host__ __device__ inline double* tile_ptr(const TileMap& m, int i, int j) {
+  if (m.packed) return m.base + packed_tile_index(i, j, m.Ym) * (i64)m.nb * m.nb;
+  return m.base + (i64)i * m.nb + (i64)j * m.nb * m.ld;
+}
+
+// A single column of tiles: tile i starts at base + i*stride (stride in elements).
+struct TileCol {
+  const double* base;
+  i64 ld;
+  i64 stride;
+};
+
+#define OOC_CUDA_TRY(expr)                                              \
+  do {                                                                  \
+    cudaError_t _e = (expr);                                            \
+    if (_e != cudaSuccess) {                                            \
+      ooc_set_last_error(_e, #expr, __FILE__, __LINE__);                \
+      return OOC_ERR_CUDA;                                              \
+    }                                                                   \
+  } while (0)
+
+void ooc_set_last_error(cudaError_t e, const char* what, const char* file, int line);
+
+// ---------------------------------------------------------------------------------
+// FP64 kernel launchers (fp64_kernels.cu).  All run on `s`, read the status word
+// `status` first and return without touching memory once it is non-zero.
+// ---------------------------------------------------------------------------------
+
+// C(i, j) -= X(i) X(j)^T for every tile pair of a trapezoid of Ht tile rows and Kt
+// tile columns (i >= j); X is a column of Ht tiles, each with K columns.  H and Kcols
+// are the element extents (the last tile row / column may be ragged).  Diagonal pairs
+// update only their lower triangle.
+int launch_panel_update(const TileCol& X, const TileMap& C, int Ht, int Kt, i64 H, i64 Kcols,
+                        int K, const int* status, cudaStream_t s);
+
+// Generic C[m x n] -= A[m x k] * B[n x k]^T (column-major, any leading dimensions);
+// lower = 1 restricts the update to the lower triangle (m == n, syrk).
+int launch_gemm_nt(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m,
+                   int n, int k, int lower, double alpha, const int* status, cudaStream_t s);
+
+// Lower Cholesky of an n x n tile in place (leading dimension ld).  On failure writes
+// status = col0 + (1-based local column) unless status is already non-zero.
+int launch_potrf_tile(double* A, i64 ld, int n, i64 col0, int* status, cudaStream_t s);
+
+// B(t) := B(t) L^-T for every tile t of a column of `ntiles` tiles with `m_last` rows in
+// the last one (all others nb rows) and n columns; L is the n x n lower tile.
+int launch_trsm_col(const double* L, i64 ldl, const TileCol& B, int ntiles, int nb, int m_last,
+                    int n, const int* status, cudaStream_t s);
+
+// ---------------------------------------------------------------------------------
+// Handle accessors shared between translation units (ooc_driver.cu).
+// ---------------------------------------------------------------------------------
+cudaStream_t ooc_compute_stream(ooc_handle* h);
+int ooc_device(ooc_handle* h);
+int ooc_wait_stream(ooc_handle* h, cudaStream_t s);  // bounded by the handle's timeout
+ooc_handle* ooc_default_handle();
+
+// Generators (matgen.cu): fill the block of global rows [r0, r0+m) and columns
+// [c0, c0+nc) of the n x n test matrix into the device buffer B (leading dimension ldb).
+int launch_gen_uniform_block(double* B, i64 ldb, i64 n, uint64_t seed, double alpha, i64 r0, i64 c0, i64 m,
+                             i64 nc, cudaStream_t s);
+int launch_gen_pdmatgen_block(double* B, i64 ldb, i64 n, int seed, i64 r0, i64 c0, i64 m, i64 nc,
+                              cudaStream_t s);

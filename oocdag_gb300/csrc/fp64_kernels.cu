@@ -1,0 +1,384 @@
+// FP64 tile kernels for the out-of-core Cholesky on GB300 (sm_103a).
+//
+// GB300 executes FP64 at about 1/1800 of its dense BF16 tensor rate: the measured
+// FP64 DMMA rate is ~1.05 TFLOP/s per GPU (about two FP64 FMAs per clock per SM).  At
+// that rate every FP64 tile operation is bound by the FP64 pipe, not by HBM or shared
+// memory, so the kernels here are built to keep the DMMA pipe issuing:
+//   * the contraction (gemm / syrk, oocquark.cpp:130,176,222 use cuBLAS there) runs on
+//     FP64 tensor-core MMAs (mma.sync m8n8k4 f64) with 64x64 output blocks per CTA,
+//     16-deep K slabs double-buffered in shared memory by cp.async;
+//   * the diagonal-tile factor (host dpotrf_ at oocquark.cpp:87 in the reference) and
+//     the column solve (cublasDtrsm at oocquark.cpp:130) are blocked into 64-wide steps
+//     so that almost all of their flops go through the same contraction kernel, with
+//     only the 64x64 diagonal pieces done in shared memory.
+// Every kernel reads the device status word first and returns at once when an earlier
+// step has reported a non-positive-definite minor.
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int BM = 64;
+constexpr int BN = 64;
+constexpr int BK = 16;
+constexpr int PAD = 4;               // row length BM+PAD makes fragment loads conflict-free
+constexpr int LDS = BM + PAD;        // shared row length (doubles)
+constexpr int GEMM_THREADS = 128;    // 4 warps in a 2 x 2 arrangement, 32 x 32 each
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void dmma884(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+// Loads rows [r0, r0+64) x columns [k0, k0+16) of the column-major operand M (rows
+// valid below `rows`, columns below `kmax`) into S[k][r] (row length LDS).
+template <bool VEC>
+__device__ __forceinline__ void load_slab(double* S, const double* M, i64 ld, int r0, int rows,
+                                          int k0, int kmax) {
+  const int t = threadIdx.x;
+  if (VEC) {
+#pragma unroll
+    for (int it = 0; it < (BM * BK / 2) / GEMM_THREADS; it++) {
+      int idx = t + it * GEMM_THREADS;
+      int kc = idx / (BM / 2);
+      int r = (idx % (BM / 2)) * 2;
+      int gr = r0 + r, gk = k0 + kc;
+      int nvalid = 0;
+      if (gk < kmax) nvalid = min(max(rows - gr, 0), 2);
+      const double* src = (nvalid > 0) ? (M + gr + (i64)gk * ld) : M;
+      cp_async16(S + kc * LDS + r, src, nvalid * 8);
+    }
+  } else {
+    for (int idx = t; idx < BM * BK; idx += GEMM_THREADS) {
+      int kc = idx / BM;
+      int r = idx % BM;
+      int gr = r0 + r, gk = k0 + kc;
+      S[kc * LDS + r] = (gr < rows && gk < kmax) ? M[gr + (i64)gk * ld] : 0.0;
+    }
+  }
+}
+
+// C[m0:m0+64, n0:n0+64] += alpha * A[m0:, 0:k] * B[n0:, 0:k]^T, restricted to the lower
+// triangle (row >= column) when `lower` is set.
+template <bool VEC>
+__device__ __forceinline__ void gemm_block(const double* __restrict__ A, i64 lda,
+                                           const double* __restrict__ B, i64 ldb,
+                                           double* __restrict__ C, i64 ldc, int m, int n, int k,
+                                           int m0, int n0, int lower, double alpha) {
+  __shared__ __align__(16) double As[2][BK * LDS];
+  __shared__ __align__(16) double Bs[2][BK * LDS];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wm = warp & 1, wn = warp >> 1;
+  const int g = lane >> 2, tig = lane & 3;
+
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+  const int nslab = (k + BK - 1) / BK;
+  if (nslab > 0) {
+    load_slab<VEC>(As[0], A, lda, m0, m, 0, k);
+    load_slab<VEC>(Bs[0], B, ldb, n0, n, 0, k);
+    if (VEC) cp_async_commit();
+  }
+  for (int s = 0; s < nslab; s++) {
+    const int cur = s & 1;
+    if (s + 1 < nslab) {
+      load_slab<VEC>(As[cur ^ 1], A, lda, m0, m, (s + 1) * BK, k);
+      load_slab<VEC>(Bs[cur ^ 1], B, ldb, n0, n, (s + 1) * BK, k);
+      if (VEC) { cp_async_commit(); cp_async_wait<1>(); }
+    } else {
+      if (VEC) cp_async_wait<0>();
+    }
+    __syncthreads();
+    const double* as = As[cur];
+    const double* bs = Bs[cur];
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 4) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = as[(kk + tig) * LDS + wm * 32 + i * 8 + g];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = bs[(kk + tig) * LDS + wn * 32 + j * 8 + g];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) dmma884(acc[i][j][0], acc[i][j][1], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int r = m0 + wm * 32 + i * 8 + g;
+    if (r >= m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = n0 + wn * 32 + j * 8 + 2 * tig + h;
+        if (c >= n || (lower && c > r)) continue;
+        double* p = C + r + (i64)c * ldc;
+        *p = fma(alpha, acc[i][j][h], *p);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Panel update: every tile pair (i >= j) of a trapezoid, one launch per X column.
+// grid.x = 64x64 blocks within a tile, grid.y = tile pair.
+// ---------------------------------------------------------------------------------
+template <bool VEC>
+__global__ void __launch_bounds__(GEMM_THREADS)
+k_panel_update(TileCol X, TileMap Cm, int Ht, int Kt, i64 H, i64 Kcols, int K, const int* status) {
+  if (status && *(volatile const int*)status) return;
+  int p = blockIdx.y;
+  int j = 0;
+  while (j < Kt && p >= Ht - j) { p -= Ht - j; j++; }
+  if (j >= Kt) return;
+  const int i = j + p;
+  const int nb = Cm.nb;
+  const int LM = (int)min((i64)nb, H - (i64)i * nb);
+  const int LN = (int)min((i64)nb, Kcols - (i64)j * nb);
+  const int mblocks = (nb + BM - 1) / BM;
+  const int m0 = (blockIdx.x % mblocks) * BM;
+  const int n0 = (blockIdx.x / mblocks) * BN;
+  if (m0 >= LM || n0 >= LN) return;
+  const int lower = (i == j);
+  if (lower && n0 > m0 + BM - 1) return;
+  const double* Xi = X.base + (i64)i * X.stride;
+  const double* Xj = X.base + (i64)j * X.stride;
+  double* Cij = tile_ptr(Cm, i, j);
+  gemm_block<VEC>(Xi, X.ld, Xj, X.ld, Cij, Cm.ld, LM, LN, K, m0, n0, lower, -1.0);
+}
+
+// ---------------------------------------------------------------------------------
+// Batched generic NT gemm: C_z += alpha A_z B_z^T, z = blockIdx.y; the last batch entry
+// may have a different row count (m_last).
+// ---------------------------------------------------------------------------------
+struct GemmBatch {
+  const double* A; i64 lda, sA;
+  const double* B; i64 ldb, sB;
+  double* C; i64 ldc, sC;
+  int m, m_last, n, k, lower, batch;
+  double alpha;
+};
+
+template <bool VEC>
+__global__ void __launch_bounds__(GEMM_THREADS) k_gemm_batched(GemmBatch gb, const int* status) {
+  if (status && *(volatile const int*)status) return;
+  const int z = blockIdx.y;
+  const int m = (z == gb.batch - 1) ? gb.m_last : gb.m;
+  const int mblocks = (max(gb.m, gb.m_last) + BM - 1) / BM;
+  const int m0 = (blockIdx.x % mblocks) * BM;
+  const int n0 = (blockIdx.x / mblocks) * BN;
+  if (m0 >= m || n0 >= gb.n) return;
+  if (gb.lower && n0 > m0 + BM - 1) return;
+  gemm_block<VEC>(gb.A + (i64)z * gb.sA, gb.lda, gb.B + (i64)z * gb.sB, gb.ldb,
+                  gb.C + (i64)z * gb.sC, gb.ldc, m, gb.n, gb.k, m0, n0, gb.lower, gb.alpha);
+}
+
+// ---------------------------------------------------------------------------------
+// Unblocked lower Cholesky of an n x n block (n <= 64) in shared memory, right-looking.
+// LAPACK convention: a pivot that is not > 0 (or is NaN) stops the factorization and
+// reports info = col0 + j + 1.
+// ---------------------------------------------------------------------------------
+constexpr int SB = 64;
+
+__global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i64 col0, int* status) {
+  if (*(volatile int*)status) return;
+  __shared__ double S[SB][SB + 1];  // S[col][row]
+  __shared__ int failed;
+  const int t = threadIdx.x;
+  for (int idx = t; idx < n * n; idx += blockDim.x) {
+    int c = idx / n, r = idx % n;
+    if (r >= c) S[c][r] = A[r + (i64)c * ld];
+  }
+  if (t == 0) failed = 0;
+  __syncthreads();
+  for (int j = 0; j < n; j++) {
+    if (t == 0) {
+      double d = S[j][j];
+      if (!(d > 0.0)) {
+        failed = 1;
+        atomicCAS(status, 0, (int)(col0 + j + 1));
+      } else {
+        S[j][j] = sqrt(d);
+      }
+    }
+    __syncthreads();
+    if (failed) break;
+    const double inv = 1.0 / S[j][j];
+    for (int r = j + 1 + t; r < n; r += blockDim.x) S[j][r] *= inv;
+    __syncthreads();
+    const int w = n - j - 1;  // trailing (w x w) lower triangle
+    for (int idx = t; idx < w * w; idx += blockDim.x) {
+      int c = j + 1 + idx / w, r = j + 1 + idx % w;
+      if (r >= c) S[c][r] -= S[j][r] * S[j][c];
+    }
+    __syncthreads();
+  }
+  // Columns factored before a failure are written back as well (LAPACK leaves the
+  // leading part of the factor in place).
+  for (int idx = t; idx < n * n; idx += blockDim.x) {
+    int c = idx / n, r = idx % n;
+    if (r >= c) A[r + (i64)c * ld] = S[c][r];
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// B := B L^-T for a block of up to 64 columns: L is n x n lower (n <= 64), B rows are
+// independent.  One thread per row, 64 rows per CTA; z = blockIdx.y walks a batch of
+// row panels (tiles) with stride sB, the last of which has m_last rows.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(64) k_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB,
+                                                   int m, int m_last, int batch, int n,
+                                                   const int* status) {
+  if (status && *(volatile const int*)status) return;
+  extern __shared__ double smem[];
+  double* Ls = smem;             // Ls[c * SB + r] = L(r, c)
+  double* Xs = smem + SB * SB;   // Xs[c * 64 + row]
+  const int t = threadIdx.x;
+  const int z = blockIdx.y;
+  const int mz = (z == batch - 1) ? m_last : m;
+  const int r0 = blockIdx.x * 64;
+  if (r0 >= mz) return;
+  double* Bz = B + (i64)z * sB;
+  for (int idx = t; idx < n * n; idx += 64) {
+    int c = idx / n, r = idx % n;
+    Ls[c * SB + r] = (r >= c) ? L[r + (i64)c * ldl] : 0.0;
+  }
+  const int row = r0 + t;
+  const bool live = row < mz;
+  for (int c = 0; c < n; c++) Xs[c * 64 + t] = live ? Bz[row + (i64)c * ldb] : 0.0;
+  __syncthreads();
+  // x_c = (b_c - sum_{q<c} x_q L(c,q)) / L(c,c)
+  for (int c = 0; c < n; c++) {
+    double v = Xs[c * 64 + t];
+    for (int q = 0; q < c; q++) v = fma(-Xs[q * 64 + t], Ls[q * SB + c], v);
+    Xs[c * 64 + t] = v / Ls[c * SB + c];
+  }
+  if (live)
+    for (int c = 0; c < n; c++) Bz[row + (i64)c * ldb] = Xs[c * 64 + t];
+}
+
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+}  // namespace
+
+// =================================================================================
+// Launchers
+// =================================================================================
+
+int launch_panel_update(const TileCol& X, const TileMap& C, int Ht, int Kt, i64 H, i64 Kcols, int K,
+                        const int* status, cudaStream_t s) {
+  if (Ht <= 0 || Kt <= 0 || K <= 0) return OOC_OK;
+  i64 npairs = (i64)Kt * Ht - ((i64)Kt * (Kt - 1)) / 2;
+  if (npairs > 65535) return OOC_ERR_INTERNAL;  // a panel never has that many tile pairs
+  const int mblocks = (C.nb + BM - 1) / BM;
+  const int nblocks = (C.nb + BN - 1) / BN;
+  dim3 grid(mblocks * nblocks, (unsigned)npairs);
+  bool vec = aligned16(X.base) && aligned16(C.base) && (X.ld % 2 == 0) && (C.ld % 2 == 0) &&
+             (X.stride % 2 == 0);
+  if (vec) k_panel_update<true><<<grid, GEMM_THREADS, 0, s>>>(X, C, Ht, Kt, H, Kcols, K, status);
+  else k_panel_update<false><<<grid, GEMM_THREADS, 0, s>>>(X, C, Ht, Kt, H, Kcols, K, status);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+static int launch_gemm_batched(const GemmBatch& gb, const int* status, cudaStream_t s) {
+  if (gb.batch <= 0 || gb.n <= 0 || (gb.m <= 0 && gb.m_last <= 0)) return OOC_OK;
+  if (gb.batch > 65535) return OOC_ERR_INTERNAL;
+  const int mb = (max(gb.m, gb.m_last) + BM - 1) / BM;
+  const int nbk = (gb.n + BN - 1) / BN;
+  dim3 grid(mb * nbk, gb.batch);
+  bool vec = aligned16(gb.A) && aligned16(gb.B) && aligned16(gb.C) && gb.lda % 2 == 0 &&
+             gb.ldb % 2 == 0 && gb.sA % 2 == 0 && gb.sB % 2 == 0;
+  if (gb.k <= 0) return OOC_OK;
+  if (vec) k_gemm_batched<true><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
+  else k_gemm_batched<false><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+int launch_gemm_nt(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m, int n,
+                   int k, int lower, double alpha, const int* status, cudaStream_t s) {
+  GemmBatch gb{A, lda, 0, B, ldb, 0, C, ldc, 0, m, m, n, k, lower, 1, alpha};
+  return launch_gemm_batched(gb, status, s);
+}
+
+static int trsm_small_smem() { return (SB * SB + SB * 64) * (int)sizeof(double); }
+
+static int launch_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB, int m, int m_last,
+                             int batch, int n, const int* status, cudaStream_t s) {
+  if (batch <= 0 || n <= 0) return OOC_OK;
+  static bool attr_set = false;  // per process; the attribute is per function
+  if (!attr_set) {
+    OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      trsm_small_smem()));
+    attr_set = true;
+  }
+  dim3 grid((max(m, m_last) + 63) / 64, batch);
+  k_trsm_small<<<grid, 64, trsm_small_smem(), s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+int launch_potrf_tile(double* A, i64 ld, int n, i64 col0, int* status, cudaStream_t s) {
+  for (int k = 0; k < n; k += SB) {
+    const int kb = min(SB, n - k);
+    double* Akk = A + k + (i64)k * ld;
+    k_potrf_small<<<1, 256, 0, s>>>(Akk, ld, kb, col0 + k, status);
+    OOC_CUDA_TRY(cudaGetLastError());
+    const int rest = n - k - kb;
+    if (rest > 0) {
+      double* Bp = A + (k + kb) + (i64)k * ld;  // rows below the block, columns k..k+kb
+      int rc = launch_trsm_small(Akk, ld, Bp, ld, 0, rest, rest, 1, kb, status, s);
+      if (rc) return rc;
+      double* Ct = A + (k + kb) + (i64)(k + kb) * ld;
+      rc = launch_gemm_nt(Bp, ld, Bp, ld, Ct, ld, rest, rest, kb, 1, -1.0, status, s);
+      if (rc) return rc;
+    }
+  }
+  return OOC_OK;
+}
+
+int launch_trsm_col(const double* L, i64 ldl, const TileCol& B, int ntiles, int nb, int m_last, int n,
+                    const int* status, cudaStream_t s) {
+  if (ntiles <= 0) return OOC_OK;
+  double* Bb = const_cast<double*>(B.base);
+  for (int k = 0; k < n; k += SB) {
+    const int kb = min(SB, n - k);
+    const double* Lkk = L + k + (i64)k * ldl;
+    int rc = launch_trsm_small(Lkk, ldl, Bb + (i64)k * B.ld, B.ld, B.stride, nb, m_last, ntiles, kb,
+                               status, s);
+    if (rc) return rc;
+    const int rest = n - k - kb;
+    if (rest > 0) {
+      // B[:, k+kb:n] -= B[:, k:k+kb] L[k+kb:n, k:k+kb]^T for every tile of the column.
+      GemmBatch gb{Bb + (i64)k * B.ld, B.ld, B.stride,
+                   L + (k + kb) + (i64)k * ldl, ldl, 0,
+                   Bb + (i64)(k + kb) * B.ld, B.ld, B.stride,
+                   nb, m_last, rest, kb, 0, ntiles, -1.0};
+      rc = launch_gemm_batched(gb, status, s);
+      if (rc) return rc;
+    }
+  }
+  return OOC_OK;
+}
