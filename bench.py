@@ -39,6 +39,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Cholesky TFLOP/s (n^3/3 flops), mixed vs FP64 at backward err<=1e-14; p99 ms"
 
+# DRAM bytes per algorithmic flop of k_panel_update, from one ncu capture of two launches
+# at n=8192, nb=1024 (dram__bytes_read.sum + dram__bytes_write.sum = 348.1 MB for
+# 44.02 GFLOP; profiles/k_panel_update_fp64_n8192.md).  The kernel's traffic is the
+# operand and C tiles, which scale with the flops of a launch at fixed nb.
+UPDATE_DRAM_BYTES_PER_FLOP = 348.1e6 / 44.02e9
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -318,7 +324,9 @@ def run_ours(args):
                                "MEASURED_PEAKS.json has no FP64 entry",
                 "launches": upd_launch, "avg_launch_ms": upd_ms / max(1, upd_launch),
                 "share_of_step": upd_ms / (ms_local * args.steps) if ms_local > 0 else None,
-                "traffic": None}
+                "traffic": (UPDATE_DRAM_BYTES_PER_FLOP * upd_flops / upd_launch) if upd_launch else None,
+                "traffic_unit": "bytes per launch (ncu capture at n=8192 scaled by flops per launch)",
+                "algorithmic_bytes_note": "operand tiles read once + C tiles read and written"}
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------------
     cpu = None

@@ -131,19 +131,23 @@ __global__ void k_lower_copy(const double* L, i64 ldl, double* Z, i64 ldz, i64 n
   }
 }
 
-// FP64 DMMA issue loop for the peak probe.
-__global__ void k_dmma_probe(double* out, int iters) {
+// FP64 DMMA issue loop for the peak probe: eight independent accumulator chains per
+// thread so that MMA latency is hidden and only the pipe's issue rate remains.
+__global__ void __launch_bounds__(256) k_dmma_probe(double* out, int iters) {
   double a = 1.0 + threadIdx.x * 1e-6, b = 1.0 - threadIdx.x * 1e-6;
-  double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double c[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) c[q] = 0.0;
   for (int i = 0; i < iters; i++) {
 #pragma unroll
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < 8; q++)
       asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
                    : "+d"(c[2 * q]), "+d"(c[2 * q + 1])
                    : "d"(a), "d"(b));
   }
   double s = 0;
-  for (int q = 0; q < 8; q++) s += c[q];
+#pragma unroll
+  for (int q = 0; q < 16; q++) s += c[q];
   out[(i64)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
@@ -346,7 +350,7 @@ extern "C" int ooc_fp64_peak_probe(ooc_handle* h, double ms, double* tflops) {
   cudaSetDevice(ooc_device(h));
   int dev = ooc_device(h), nsm = 0;
   OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int blocks = nsm * 4, threads = 128;
+  const int blocks = nsm * 4, threads = 256;
   double* out = nullptr;
   OOC_CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
   cudaStream_t s = ooc_compute_stream(h);
@@ -363,7 +367,7 @@ extern "C" int ooc_fp64_peak_probe(ooc_handle* h, double ms, double* tflops) {
     int rc = ooc_wait_stream(h, s);
     if (rc) { cudaFree(out); return rc; }
     cudaEventElapsedTime(&el, e0, e1);
-    double flops = 2.0 * 8 * 8 * 4 * 4.0 * iters * (double)blocks * (threads / 32);
+    double flops = 2.0 * 8 * 8 * 4 * 8.0 * iters * (double)blocks * (threads / 32);
     rate = flops / (el * 1e-3) / 1e12;
     if (el >= ms) break;
     iters = (int)std::min(1e8, iters * std::max(2.0, ms / std::max(el, 1e-3f) * 1.1));
