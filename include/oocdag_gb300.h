@@ -103,6 +103,28 @@ void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, cons
  * Returns the number of panels, OOC_ERR_BUDGET, or -5 if cap triples do not suffice. */
 int ooc_panel_plan(int64_t n, int nb, int64_t memBlock, int nx, int* out, int cap);
 
+/* Size of the device array that ooc_dpotrf_L_static uses as its panel buffer.      */
+#define OOC_STATIC_PANEL_BYTES (64u << 20)
+
+/* Out-of-core lower Cholesky that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: processes whose device memory belongs to
+ * another allocator (a framework's caching pool that has reserved the GPU, where a new
+ * allocation fails or fragments it), and servers that must not let an allocation or a
+ * free synchronize the device under their other streams.  The panel buffer and status
+ * word live in the library's static device memory (OOC_STATIC_PANEL_BYTES, held by every
+ * GPU that loads the library until exit); all work runs on `stream` (a cudaStream_t,
+ * NULL = the legacy default stream).  A: host (pageable or page-locked) or device,
+ * column-major, lower triangle factored in place as ooc_dpotrf_L does.
+ * - Limit: the matrix must fit the reference's panel rule in OOC_STATIC_PANEL_BYTES with
+ *   one X buffer (about 2*ceil(n/nb)+1 tiles of nb*nb doubles); larger sizes return
+ *   OOC_ERR_BUDGET with a message in ooc_last_error_string().
+ * - The first call on a device looks up the array's device address (set-up); make that
+ *   first call before any stream capture.
+ * - Calls share the array: the status word is cleared at the start of each call; calls
+ *   whose GPU work overlaps (e.g. two threads on two streams) race and must be
+ *   serialized by the caller.                                                        */
+int ooc_dpotrf_L_static(double* A, int64_t n, int64_t lda, int nb, void* stream, int* info);
+
 /* ---- test matrices (the reference's generator, and the uniform generator) ------ */
 /* pdmatgen('Symm','Diag') on a 1 x 1 grid (LIN/pdmatgen.f, called at oocdag.cpp:298-302):
  * A(i,j) = 1 - 2 u[min(i,j) n + max(i,j)], A(i,i) = |A(i,i)| + n, u from the 31-bit LCG

@@ -78,6 +78,7 @@ def header_functions() -> list[str]:
         text = open(os.path.join(inc, fn)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = re.sub(r"//[^\n]*", "", text)
+        text = re.sub(r"^\s*#[^\n]*", "", text, flags=re.M)
         for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text):
             name = m.group(1)
             if name not in ("if", "while", "for", "return", "sizeof"):
@@ -117,6 +118,7 @@ def load(build_if_missing: bool = True):
     L.ooc_fp64_peak_probe.argtypes = [P, D, ctypes.POINTER(D)]
     L.ooc_panel_plan.argtypes = [I64, I, I64, I, ctypes.POINTER(I), I]
     L.ooc_get_stream.argtypes = [P, I, ctypes.POINTER(P)]
+    L.ooc_dpotrf_L_static.argtypes = [P, I64, I64, I, P, ctypes.POINTER(I)]
     _lib = L
     return L
 
@@ -247,4 +249,14 @@ def pdpotrf(uplo: str, n: int, A, ia: int, ja: int, desca) -> int:
     info = ctypes.c_int(0)
     L.ooc_pdpotrf_(uplo.encode(), ctypes.byref(ctypes.c_int(n)), _ptr(A), ctypes.byref(ctypes.c_int(ia)),
                    ctypes.byref(ctypes.c_int(ja)), d, ctypes.byref(info))
+    return info.value
+
+
+def dpotrf_L_static(A, n: int, lda: int, nb: int, stream: int = 0) -> int:
+    """Allocation-free out-of-core Cholesky (ooc_dpotrf_L_static): the panel buffer is the
+    library's fixed static device array, the work runs on `stream`.  Returns LAPACK info;
+    raises OocError (OOC_ERR_BUDGET) when the matrix does not fit the static buffer."""
+    info = ctypes.c_int(0)
+    _check(load().ooc_dpotrf_L_static(_ptr(A), n, lda, nb, stream or None, ctypes.byref(info)),
+           "ooc_dpotrf_L_static")
     return info.value

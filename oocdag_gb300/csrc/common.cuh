@@ -49,6 +49,7 @@ struct TileCol {
   } while (0)
 
 void ooc_set_last_error(cudaError_t e, const char* what, const char* file, int line);
+void ooc_set_last_message(const char* msg);
 
 // ---------------------------------------------------------------------------------
 // FP64 kernel launchers (fp64_kernels.cu).  All run on `s`, read the status word

@@ -47,6 +47,8 @@ void ooc_set_last_error(cudaError_t e, const char* what, const char* file, int l
   g_last_error = buf;
 }
 
+void ooc_set_last_message(const char* msg) { g_last_error = msg; }
+
 extern "C" const char* ooc_last_error_string(void) { return g_last_error.c_str(); }
 
 // ---------------------------------------------------------------------------------
