@@ -103,6 +103,43 @@ void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, cons
  * Returns the number of panels, OOC_ERR_BUDGET, or -5 if cap triples do not suffice. */
 int ooc_panel_plan(int64_t n, int nb, int64_t memBlock, int nx, int* out, int cap);
 
+/* ---- mixed precision: factor once, solve with FP64 iterative refinement -------- */
+/* Precision of the trailing syrk/gemm updates (the diagonal-tile potrf and the column
+ * solve always run in FP64).                                                        */
+enum {
+  OOC_PREC_FP64 = 0,  /* FP64 DMMA updates (the plain path)                        */
+  OOC_PREC_FP32 = 1,  /* FP32 operands, FP32 FFMA accumulation                      */
+  OOC_PREC_BF16X3 = 2 /* hi/lo BF16 splits, 3 tensor-core products, FP32 accumulate */
+};
+
+typedef struct ooc_factor ooc_factor;
+
+/* Factor an SPD matrix in core (A: host or device, lower triangle read; A is not
+ * modified) with trailing updates in `prec`; keeps L, the inverses of its diagonal
+ * tiles and (for prec != FP64) FP32 copies for refinement.  No reference counterpart:
+ * the reference only factors (oocdag.cpp:18) and checks with dpotrs (oocdag.cpp:439). */
+int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int64_t lda, int nb, int prec,
+                      ooc_factor** F, int* info, ooc_stats* stats);
+int ooc_factor_destroy(ooc_factor* F);
+/* Copy the factor (lower triangle = L; the upper triangle holds A's values) out.      */
+int ooc_factor_copy_L(ooc_factor* F, double* L, int64_t ldl);
+/* B := A^{-1} B with the factor (FP64 triangular solves), B on the device, nrhs <= 16.
+ * The dpotrs of the reference's VERIFY block (oocdag.cpp:439).                       */
+int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t ldb, int nrhs);
+/* Solve A X = B by iterative refinement: X0 from the factor, then R = B - A X in FP64
+ * with the original A (device), correction with the factor (FP32 copy for a reduced-
+ * precision factor), until the normwise backward error ||R||_inf/(||A||_inf ||X||_inf
+ * + ||B||_inf) <= tol or maxiter corrections.  B, X: device, nrhs <= 16.             */
+int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda, const double* B,
+                     int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
+                     double* berr);
+
+/* C := C - A A^T on the lower triangle (device pointers; A n x k), with the trailing-
+ * update kernel of precision `prec`: the dsyrk('L','N',-1,A,1,C) task body of the
+ * reference (oocquark.cpp:176, cublasDsyrk_v2) as a tile call.                       */
+int ooc_dsyrk_ln(ooc_handle* h, int prec, int n, int k, const double* A, int64_t lda, double* C,
+                 int64_t ldc);
+
 /* Size of the device array that ooc_dpotrf_L_static uses as its panel buffer.      */
 #define OOC_STATIC_PANEL_BYTES (64u << 20)
 

@@ -35,6 +35,11 @@ OPT_PROFILE = 3
 OPT_PIN_HOST = 4
 OPT_REF_SCHEDULE = 5
 
+PREC_FP64 = 0
+PREC_FP32 = 1
+PREC_BF16X3 = 2
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "bf16x3": PREC_BF16X3}
+
 
 class OocError(RuntimeError):
     def __init__(self, code: int, where: str):
@@ -119,6 +124,13 @@ def load(build_if_missing: bool = True):
     L.ooc_panel_plan.argtypes = [I64, I, I64, I, ctypes.POINTER(I), I]
     L.ooc_get_stream.argtypes = [P, I, ctypes.POINTER(P)]
     L.ooc_dpotrf_L_static.argtypes = [P, I64, I64, I, P, ctypes.POINTER(I)]
+    L.ooc_factor_create.argtypes = [P, P, I64, I64, I, I, ctypes.POINTER(P), ctypes.POINTER(I),
+                                    ctypes.POINTER(OocStats)]
+    L.ooc_factor_destroy.argtypes = [P]
+    L.ooc_dsyrk_ln.argtypes = [P, I, I, I, P, I64, P, I64]
+    L.ooc_factor_copy_L.argtypes = [P, P, I64]
+    L.ooc_factor_solve.argtypes = [P, P, P, I64, I]
+    L.ooc_solve_refine.argtypes = [P, P, P, I64, P, I64, P, I64, I, D, I, ctypes.POINTER(I), ctypes.POINTER(D)]
     _lib = L
     return L
 
@@ -222,6 +234,22 @@ class Handle:
                "ooc_dresidual")
         return r.value
 
+    def factor(self, A, n: int, lda: int, nb: int, prec="fp64") -> "Factor":
+        """In-core factorization with trailing updates in `prec` ('fp64', 'fp32',
+        'bf16x3'); A (host or device) is left unchanged."""
+        p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+        F = ctypes.c_void_p()
+        info = ctypes.c_int(0)
+        st = OocStats()
+        _check(load().ooc_factor_create(self._h, _ptr(A), n, lda, nb, p, ctypes.byref(F), ctypes.byref(info),
+                                        ctypes.byref(st)), "ooc_factor_create")
+        return Factor(self, F, n, info.value, st.as_dict())
+
+    def dsyrk_ln(self, prec, n: int, k: int, A, lda: int, C, ldc: int) -> None:
+        """C := C - A A^T (lower) on the device with the given update precision."""
+        p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+        _check(load().ooc_dsyrk_ln(self._h, p, n, k, _ptr(A), lda, _ptr(C), ldc), "ooc_dsyrk_ln")
+
     def fp64_peak(self, ms: float = 200.0) -> float:
         r = ctypes.c_double()
         _check(load().ooc_fp64_peak_probe(self._h, float(ms), ctypes.byref(r)), "ooc_fp64_peak_probe")
@@ -260,3 +288,47 @@ def dpotrf_L_static(A, n: int, lda: int, nb: int, stream: int = 0) -> int:
     _check(load().ooc_dpotrf_L_static(_ptr(A), n, lda, nb, stream or None, ctypes.byref(info)),
            "ooc_dpotrf_L_static")
     return info.value
+
+
+class Factor:
+    """A factor kept on the device for repeated solves (ooc_factor)."""
+
+    def __init__(self, handle: Handle, ptr, n: int, info: int, stats: dict):
+        self.handle = handle
+        self._f = ptr
+        self.n = n
+        self.info = info
+        self.stats = stats
+
+    def close(self) -> None:
+        if self._f:
+            load().ooc_factor_destroy(self._f)
+            self._f = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def copy_L(self, L, ldl: int) -> None:
+        _check(load().ooc_factor_copy_L(self._f, _ptr(L), ldl), "ooc_factor_copy_L")
+
+    def solve(self, B, ldb: int, nrhs: int) -> None:
+        """B := A^{-1} B in FP64 (device B)."""
+        _check(load().ooc_factor_solve(self.handle.ptr, self._f, _ptr(B), ldb, nrhs), "ooc_factor_solve")
+
+    def refine(self, A, lda: int, B, ldb: int, X, ldx: int, nrhs: int, tol: float = 1e-14, maxiter: int = 30):
+        """Iterative refinement to backward error <= tol; returns (iterations, backward error)."""
+        it = ctypes.c_int(0)
+        be = ctypes.c_double(0)
+        _check(load().ooc_solve_refine(self.handle.ptr, self._f, _ptr(A), lda, _ptr(B), ldb, _ptr(X), ldx, nrhs,
+                                       float(tol), int(maxiter), ctypes.byref(it), ctypes.byref(be)),
+               "ooc_solve_refine")
+        return it.value, be.value

@@ -1,0 +1,827 @@
+// Mixed-precision factorization and FP64 solves with iterative refinement.
+//
+// The factorization keeps the structure of the plain path (diagonal-tile potrf and the
+// column solve in FP64, oocquark.cpp:393-410 in the reference) but runs the trailing
+// syrk/gemm updates (oocquark.cpp:346,351) in reduced precision:
+//   OOC_PREC_FP32  : FP32 copies of the column panel, FP32 FFMA products accumulated in
+//                    FP32, subtracted from the FP64 trailing matrix;
+//   OOC_PREC_BF16X3: hi/lo BF16 splits of the column panel, three tensor-core products
+//                    (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM (tc_bf16x3.cu).
+// The factor is then used for a solve whose residuals are computed in FP64 against the
+// untouched FP64 matrix, refining the solution until the normwise backward error
+// ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches the requested tolerance.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------------
+// FP32 lower-triangular rank-K update: C (FP64, lower) -= X X^T with X (m x K, FP32,
+// column-major, ld ldx).  128 x 128 output blocks, lower-triangular block grid.
+// ---------------------------------------------------------------------------------
+constexpr int FB = 128, FK = 16, FTHR = 256;
+
+__device__ __forceinline__ void cp_async16f(void* smem, const void* gmem, int src_bytes) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
+
+__device__ __forceinline__ void tri_decode(int t, int* bi, int* bj) {
+  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((i + 1) * (i + 2) / 2 <= t) i++;
+  while (i * (i + 1) / 2 > t) i--;
+  *bi = i;
+  *bj = t - i * (i + 1) / 2;
+}
+
+__device__ __forceinline__ void load_slab_f32(float* S, const float* X, i64 ldx, int r0, int m, int k0, int K) {
+  // 128 rows x 16 k; each k column holds 128 contiguous floats = 32 x 16 B.
+  for (int idx = threadIdx.x; idx < FK * (FB / 4); idx += FTHR) {
+    const int kc = idx / (FB / 4);
+    const int r = (idx % (FB / 4)) * 4;
+    const int gr = r0 + r, gk = k0 + kc;
+    int nv = 0;
+    if (gk < K) nv = min(max(m - gr, 0), 4);
+    const float* src = nv > 0 ? X + gr + (i64)gk * ldx : X;
+    cp_async16f(S + kc * FB + r, src, nv * 4);
+  }
+}
+
+__global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, i64 ldx, double* __restrict__ C,
+                                                   i64 ldc, int m, int K, const int* status) {
+  if (status && *(volatile const int*)status) return;
+  int bi, bj;
+  tri_decode(blockIdx.x, &bi, &bj);
+  const int m0 = bi * FB, n0 = bj * FB;
+  // 32 KB: double-buffered A and B slabs, reused afterwards to stage the result.
+  __shared__ __align__(16) float smem[4 * FK * FB];
+  float* As[2] = {smem, smem + FK * FB};
+  float* Bs[2] = {smem + 2 * FK * FB, smem + 3 * FK * FB};
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+  const int nslab = (K + FK - 1) / FK;
+  load_slab_f32(As[0], X, ldx, m0, m, 0, K);
+  load_slab_f32(Bs[0], X, ldx, n0, m, 0, K);
+  asm volatile("cp.async.commit_group;\n" ::);
+  for (int s = 0; s < nslab; s++) {
+    const int cur = s & 1;
+    if (s + 1 < nslab) {
+      load_slab_f32(As[cur ^ 1], X, ldx, m0, m, (s + 1) * FK, K);
+      load_slab_f32(Bs[cur ^ 1], X, ldx, n0, m, (s + 1) * FK, K);
+      asm volatile("cp.async.commit_group;\n" ::);
+      asm volatile("cp.async.wait_group 1;\n" ::);
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::);
+    }
+    __syncthreads();
+    const float* as = As[cur];
+    const float* bs = Bs[cur];
+#pragma unroll
+    for (int k = 0; k < FK; k++) {
+      const float4 a0 = *reinterpret_cast<const float4*>(as + k * FB + ty * 4);
+      const float4 a1 = *reinterpret_cast<const float4*>(as + k * FB + 64 + ty * 4);
+      const float4 b0 = *reinterpret_cast<const float4*>(bs + k * FB + tx * 4);
+      const float4 b1 = *reinterpret_cast<const float4*>(bs + k * FB + 64 + tx * 4);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  // Stage the block through shared memory, 32 columns at a time (stride 129 floats),
+  // so that the FP64 read-modify-write of C walks whole columns (coalesced).
+  // Thread columns: quarter 0 = tx*4+j for tx < 8, quarter 1 = tx*4+j for tx >= 8,
+  // quarters 2/3 the same shifted by 64.
+  float* stage = smem;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int qtr = 0; qtr < 4; qtr++) {
+    const int half = qtr >> 1;      // which group of 4 accumulator columns
+    const int lo_tx = (qtr & 1) * 8;  // threads whose columns fall in this quarter
+    if (tx >= lo_tx && tx < lo_tx + 8) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int rr = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int cc = (tx - lo_tx) * 4 + j;  // 0..31 inside this quarter
+          stage[cc * 129 + rr] = acc[i][half * 4 + j];
+        }
+      }
+    }
+    __syncthreads();
+    for (int cc = warp; cc < 32; cc += FTHR / 32) {
+      const int c = n0 + half * 64 + (qtr & 1) * 32 + cc;
+      if (c >= m) continue;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int rr = lane + 32 * q;
+        const int r = m0 + rr;
+        if (r >= m || (bi == bj && c > r)) continue;
+        double* p = C + r + (i64)c * ldc;
+        *p -= (double)stage[cc * 129 + rr];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// FP64 column panel (m x K, ld ldx) -> FP32 copy (ld ldy).
+__global__ void k_to_f32(const double* __restrict__ X, i64 ldx, float* __restrict__ Y, i64 ldy, int m, int K) {
+  const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  for (int k = blockIdx.y; k < K; k += gridDim.y) Y[r + k * ldy] = (float)X[r + k * ldx];
+}
+
+// ---------------------------------------------------------------------------------
+// Small-right-hand-side products (r <= 16 columns), accumulated in TC:
+//   NN:  C[m x r] = beta C + alpha A[m x k] B[k x r]        thread per row
+//   TN:  C[m x r] = beta C + alpha A[k x m]^T B[k x r]      warp per row
+// (beta is 0 or 1).  For NN the long dimension k can be split across blockIdx.y into a
+// partial buffer P (nslice x m x r) that k_reduce_slices sums in slice order, so results
+// never depend on scheduling.
+// ---------------------------------------------------------------------------------
+constexpr int RMAX = 16;
+constexpr int NN_KCHUNK = 256;
+
+template <typename TA, typename TC>
+__global__ void __launch_bounds__(256) k_gemm_nn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
+                                                       i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
+                                                       int kslice, TC* __restrict__ P, TC alpha, TC beta) {
+  __shared__ TC Bs[NN_KCHUNK * RMAX];
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k0 = blockIdx.y * kslice;
+  const int k1 = min(k, k0 + kslice);
+  TC acc[RMAX];
+#pragma unroll
+  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int kc = k0; kc < k1; kc += NN_KCHUNK) {
+    const int kn = min(NN_KCHUNK, k1 - kc);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+      const int q = idx / kn, kk = idx % kn;
+      Bs[kk * RMAX + q] = B[(kc + kk) + (i64)q * ldb];
+    }
+    __syncthreads();
+    if (row < m) {
+      for (int kk = 0; kk < kn; kk++) {
+        const TC a = (TC)A[row + (i64)(kc + kk) * lda];
+#pragma unroll
+        for (int q = 0; q < RMAX; q++)
+          if (q < r) acc[q] = fma(a, Bs[kk * RMAX + q], acc[q]);
+      }
+    }
+  }
+  if (row >= m) return;
+  if (P) {
+    TC* Pz = P + (i64)blockIdx.y * m * r;
+    for (int q = 0; q < r; q++) Pz[row + (i64)q * m] = acc[q];
+  } else {
+    for (int q = 0; q < r; q++) {
+      TC* c = C + row + (i64)q * ldc;
+      *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
+    }
+  }
+}
+
+template <typename TC>
+__global__ void k_reduce_slices(const TC* __restrict__ P, int nslice, TC* __restrict__ C, i64 ldc, int m, int r,
+                                TC alpha, TC beta) {
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= m) return;
+  for (int q = 0; q < r; q++) {
+    TC sum = 0;
+    for (int z = 0; z < nslice; z++) sum += P[(i64)z * m * r + row + (i64)q * m];
+    TC* c = C + row + (i64)q * ldc;
+    *c = (beta != TC(0)) ? fma(alpha, sum, *c) : alpha * sum;
+  }
+}
+
+template <typename TA, typename TC>
+__global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
+                                                       i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
+                                                       TC alpha, TC beta) {
+  __shared__ TC Bs[NN_KCHUNK * RMAX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const i64 row = (i64)blockIdx.x * (blockDim.x / 32) + warp;
+  TC acc[RMAX];
+#pragma unroll
+  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int kc = 0; kc < k; kc += NN_KCHUNK) {
+    const int kn = min(NN_KCHUNK, k - kc);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+      const int q = idx / kn, kk = idx % kn;
+      Bs[kk * RMAX + q] = B[(kc + kk) + (i64)q * ldb];
+    }
+    __syncthreads();
+    if (row < m) {
+      for (int kk = lane; kk < kn; kk += 32) {
+        const TC a = (TC)A[(kc + kk) + row * lda];
+#pragma unroll
+        for (int q = 0; q < RMAX; q++)
+          if (q < r) acc[q] = fma(a, Bs[kk * RMAX + q], acc[q]);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RMAX; q++) {
+    TC v = acc[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    acc[q] = v;
+  }
+  if (row >= m || lane != 0) return;
+  for (int q = 0; q < r; q++) {
+    TC* c = C + row + (i64)q * ldc;
+    *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
+  }
+}
+
+// Identity into a (n x n, ld) block.
+template <typename T>
+__global__ void k_set_identity(T* D, i64 ld, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int c = blockIdx.y; c < n; c += gridDim.y) D[r + (i64)c * ld] = (r == c) ? T(1) : T(0);
+}
+
+// Copy with conversion (column-major blocks).
+template <typename TS, typename TD>
+__global__ void k_copy_conv(const TS* __restrict__ S, i64 lds, TD* __restrict__ D, i64 ldd, int m, int n) {
+  const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  for (int c = blockIdx.y; c < n; c += gridDim.y) D[r + (i64)c * ldd] = (TD)S[r + (i64)c * lds];
+}
+
+// x += d (columns), and per-column max |.| of x, r and b for the backward error.
+__global__ void k_axpy_cols(double* X, i64 ldx, const double* D, i64 ldd, int n, int r) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) X[i + q * ldx] += D[i + q * ldd];
+}
+
+__global__ void k_colmax_abs(const double* V, i64 ld, int n, int r, double* out /* r per CTA */) {
+  __shared__ double sm[256];
+  for (int q = 0; q < r; q++) {
+    double mx = 0;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+      mx = fmax(mx, fabs(V[i + q * ld]));
+    sm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + w]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(i64)blockIdx.x * r + q] = sm[0];
+    __syncthreads();
+  }
+}
+
+// Row sums of |A| (for ||A||_inf), one thread per row.
+__global__ void k_rowsum_abs(const double* A, i64 lda, int n, double* out) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0;
+  for (int c = 0; c < n; c++) s += fabs(A[i + (i64)c * lda]);
+  out[i] = s;
+}
+
+}  // namespace
+
+// =================================================================================
+// Host-side pieces
+// =================================================================================
+
+int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
+                       cudaStream_t s, void* work, size_t work_bytes);
+size_t bf16x3_work_bytes(int m, int K);
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  int ensure(size_t b) {
+    if (bytes >= b) return OOC_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+      cudaGetLastError();
+      return OOC_ERR_NOMEM;
+    }
+    bytes = b;
+    return OOC_OK;
+  }
+};
+
+int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
+                 cudaStream_t s, DevBuf& work) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (prec == OOC_PREC_FP32) {
+    const i64 ldy = ((i64)m + 3) / 4 * 4;
+    int rc = work.ensure((size_t)ldy * K * sizeof(float));
+    if (rc) return rc;
+    float* Y = (float*)work.p;
+    k_to_f32<<<dim3((unsigned)((m + 255) / 256), (unsigned)std::min(K, 1024)), 256, 0, s>>>(X, ldx, Y, ldy, m, K);
+    const i64 T = ((i64)m + FB - 1) / FB;
+    const i64 nblk = T * (T + 1) / 2;
+    if (nblk > 0x7fffffff) return OOC_ERR_INTERNAL;
+    k_syrk_f32<<<(unsigned)nblk, FTHR, 0, s>>>(Y, ldy, C, ldc, m, K, status);
+    OOC_CUDA_TRY(cudaGetLastError());
+    return OOC_OK;
+  }
+  if (prec == OOC_PREC_BF16X3) {
+    int rc = work.ensure(bf16x3_work_bytes(m, K));
+    if (rc) return rc;
+    return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes);
+  }
+  return OOC_ERR_UNSUPPORTED;
+}
+
+template <typename TA, typename TC>
+int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, int m, int k, int r, TC alpha, TC beta,
+                  cudaStream_t s, DevBuf* part) {
+  if (m <= 0 || r <= 0) return OOC_OK;
+  if (r > RMAX) return OOC_ERR_UNSUPPORTED;
+  if (k <= 0) {
+    if (beta == TC(0)) {
+      for (int q = 0; q < r; q++) OOC_CUDA_TRY(cudaMemsetAsync(C + (i64)q * ldc, 0, sizeof(TC) * m, s));
+    }
+    return OOC_OK;
+  }
+  const int rows_blocks = (m + 255) / 256;
+  // Split the long k dimension when too few row blocks would fill the GPU.
+  int nslice = 1;
+  if (part && rows_blocks < 304 && k > 2 * NN_KCHUNK)
+    nslice = std::min((k + NN_KCHUNK - 1) / NN_KCHUNK, (304 + rows_blocks - 1) / rows_blocks);
+  if (nslice > 1) {
+    const int kslice = ((k + nslice - 1) / nslice + NN_KCHUNK - 1) / NN_KCHUNK * NN_KCHUNK;
+    nslice = (k + kslice - 1) / kslice;
+    int rc = part->ensure((size_t)nslice * m * r * sizeof(TC));
+    if (rc) return rc;
+    k_gemm_nn_small<TA, TC><<<dim3(rows_blocks, nslice), 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, kslice,
+                                                                      (TC*)part->p, alpha, beta);
+    k_reduce_slices<TC><<<rows_blocks, 256, 0, s>>>((const TC*)part->p, nslice, C, ldc, m, r, alpha, beta);
+  } else {
+    k_gemm_nn_small<TA, TC><<<dim3(rows_blocks, 1), 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, k, nullptr,
+                                                                 alpha, beta);
+  }
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+template <typename TA, typename TC>
+int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, int m, int k, int r, TC alpha, TC beta,
+                  cudaStream_t s) {
+  if (m <= 0 || r <= 0) return OOC_OK;
+  if (r > RMAX) return OOC_ERR_UNSUPPORTED;
+  k_gemm_tn_small<TA, TC><<<(m + 7) / 8, 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, alpha, beta);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+// Solve L L^T X = B in place (B: n x r, ld ldb) using the inverses of the diagonal
+// tiles.  Dinv_J holds L_JJ^{-T} (column-major, upper), i.e. the transpose of
+// L_JJ^{-1}; tmp holds nb x r.
+template <typename T>
+int solve_with(const T* L, i64 ldl, const T* Dinv, i64 n, int nb, T* B, i64 ldb, int r, T* tmp, cudaStream_t s,
+               DevBuf* part) {
+  const int bb = (int)((n + nb - 1) / nb);
+  const i64 tile = (i64)nb * nb;
+  int rc;
+  // forward: L y = b
+  for (int J = 0; J < bb; J++) {
+    const i64 J0 = (i64)J * nb;
+    const int LN = (int)std::min<i64>(nb, n - J0);
+    // y_J = L_JJ^{-1} b_J = Dinv_J^T b_J
+    rc = gemm_tn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s);
+    if (rc) return rc;
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+                                   cudaMemcpyDeviceToDevice, s));
+    const i64 rows = n - J0 - LN;
+    if (rows > 0) {
+      rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, B + J0, ldb, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
+                               T(1), s, part);
+      if (rc) return rc;
+    }
+  }
+  // backward: L^T x = y
+  for (int J = bb - 1; J >= 0; J--) {
+    const i64 J0 = (i64)J * nb;
+    const int LN = (int)std::min<i64>(nb, n - J0);
+    // x_J = L_JJ^{-T} y_J = Dinv_J y_J
+    rc = gemm_nn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s, nullptr);
+    if (rc) return rc;
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+                                   cudaMemcpyDeviceToDevice, s));
+    if (J0 > 0) {
+      // y_{<J} -= L_{J,<J}^T x_J
+      rc = gemm_tn_small<T, T>(L + J0, ldl, B + J0, ldb, B, ldb, (int)J0, LN, r, T(-1), T(1), s);
+      if (rc) return rc;
+    }
+  }
+  return OOC_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// Solver state: a factor with the inverses of its diagonal tiles (FP64), and FP32
+// copies of both for the correction solves of the refinement.
+// ---------------------------------------------------------------------------------
+struct ooc_factor {
+  int device = 0;
+  i64 n = 0;
+  int nb = 0;
+  int prec = OOC_PREC_FP64;
+  double* L = nullptr;     // n x n, ld n (owned); lower = factor
+  double* Dinv = nullptr;  // bb tiles of nb x nb: L_JJ^{-T}
+  float* Lf = nullptr;     // FP32 copy of L, ld n
+  float* Dinvf = nullptr;
+  double* tmp = nullptr;   // nb x 16
+  float* tmpf = nullptr;
+  int* status = nullptr;   // device status word of the factorization
+  int info = 0;
+  DevBuf part, partf, work;
+  ~ooc_factor() {
+    if (L) cudaFree(L);
+    if (Dinv) cudaFree(Dinv);
+    if (Lf) cudaFree(Lf);
+    if (Dinvf) cudaFree(Dinvf);
+    if (tmp) cudaFree(tmp);
+    if (tmpf) cudaFree(tmpf);
+    if (status) cudaFree(status);
+  }
+};
+
+namespace {
+
+int alloc_factor(ooc_factor* F, i64 n, int nb, bool want_f32) {
+  const int bb = (int)((n + nb - 1) / nb);
+  const size_t tiles = (size_t)bb * nb * nb;
+  if (cudaMalloc(&F->L, (size_t)n * n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&F->Dinv, tiles * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&F->tmp, (size_t)nb * RMAX * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&F->status, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return OOC_ERR_NOMEM;
+  }
+  if (want_f32) {
+    if (cudaMalloc(&F->Lf, (size_t)n * n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&F->Dinvf, tiles * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&F->tmpf, (size_t)nb * RMAX * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return OOC_ERR_NOMEM;
+    }
+  }
+  return OOC_OK;
+}
+
+// Diagonal-tile inverses: Dinv_J = I * L_JJ^{-T} through the FP64 column solve.
+int diag_inverses(ooc_factor* F, cudaStream_t s) {
+  const int nb = F->nb;
+  const int bb = (int)((F->n + nb - 1) / nb);
+  const i64 tile = (i64)nb * nb;
+  for (int J = 0; J < bb; J++) {
+    const int LN = (int)std::min<i64>(nb, F->n - (i64)J * nb);
+    double* D = F->Dinv + (i64)J * tile;
+    k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s>>>(D, nb, LN);
+    const double* LJJ = F->L + (i64)J * nb * (1 + F->n);
+    int rc = launch_trsm_col(LJJ, F->n, TileCol{D, nb, tile}, 1, LN, LN, LN, F->status, s);
+    if (rc) return rc;
+  }
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+// Right-looking in-core factorization of F->L (ld n) with FP64 potrf/trsm and trailing
+// updates in `prec` (the reference's ooc_incore over the whole matrix,
+// oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-triangular update).
+int factor_mixed(ooc_factor* F, int prec, cudaStream_t s, int64_t* launches) {
+  const i64 n = F->n;
+  const int nb = F->nb;
+  const int bb = (int)((n + nb - 1) / nb);
+  double* A = F->L;
+  const i64 lda = n;
+  for (int j = 0; j < bb; j++) {
+    const i64 J0 = (i64)j * nb;
+    const int LN = (int)std::min<i64>(nb, n - J0);
+    double* Djj = A + J0 + J0 * lda;
+    int rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s);
+    if (rc) return rc;
+    const int below = bb - j - 1;
+    if (below > 0) {
+      const int m_last = (int)(n - (i64)(bb - 1) * nb);
+      rc = launch_trsm_col(Djj, lda, TileCol{Djj + LN, lda, nb}, below, nb, m_last, LN, F->status, s);
+      if (rc) return rc;
+      const i64 m = n - J0 - LN;
+      if (prec == OOC_PREC_FP64) {
+        TileMap C{A + (J0 + LN) * (1 + lda), lda, 0, below, nb};
+        rc = launch_panel_update(TileCol{Djj + LN, lda, nb}, C, below, below, m, m, LN, F->status, s);
+      } else {
+        rc = syrk_lowprec(prec, Djj + LN, lda, A + (J0 + LN) * (1 + lda), lda, (int)m, LN, F->status, s, F->work);
+      }
+      if (rc) return rc;
+    }
+    if (launches) *launches += 6 * ((LN + 63) / 64) + 2;
+  }
+  return OOC_OK;
+}
+
+int read_int(const int* d, int* h, cudaStream_t s) {
+  OOC_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OOC_CUDA_TRY(cudaStreamSynchronize(s));
+  return OOC_OK;
+}
+
+}  // namespace
+
+extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int64_t lda, int nb, int prec,
+                                 ooc_factor** out, int* info, ooc_stats* stats) {
+  if (!h) return -1;
+  if (!A && n > 0) return -2;
+  if (n <= 0) return -3;
+  if (lda < n) return -4;
+  if (nb <= 0) return -5;
+  if (prec != OOC_PREC_FP64 && prec != OOC_PREC_FP32 && prec != OOC_PREC_BF16X3) return -6;
+  if (!out) return -7;
+  if (!info) return -8;
+  *out = nullptr;
+  *info = 0;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  ooc_factor* F = new ooc_factor();
+  F->device = ooc_device(h);
+  F->n = n;
+  F->nb = nb;
+  F->prec = prec;
+  int rc = alloc_factor(F, n, nb, prec != OOC_PREC_FP64);
+  if (rc) { delete F; return rc; }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // copy A (host or device) into the factor's storage
+  rc = OOC_OK;
+  if (cudaMemsetAsync(F->status, 0, sizeof(int), s) != cudaSuccess ||
+      cudaMemcpy2DAsync(F->L, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, cudaMemcpyDefault,
+                        s) != cudaSuccess) {
+    rc = OOC_ERR_CUDA;
+  }
+  int64_t launches = 0;
+  if (!rc) {
+    cudaEventRecord(e0, s);
+    rc = factor_mixed(F, prec, s, &launches);
+    if (!rc) rc = diag_inverses(F, s);
+    if (!rc && F->Lf) {
+      const int bb = (int)((n + nb - 1) / nb);
+      k_copy_conv<double, float><<<dim3((unsigned)((n + 255) / 256), 1024), 256, 0, s>>>(F->L, n, F->Lf, n, (int)n,
+                                                                                         (int)n);
+      k_copy_conv<double, float><<<dim3((unsigned)((nb + 255) / 256), 1024), 256, 0, s>>>(
+          F->Dinv, nb, F->Dinvf, nb, nb, bb * nb);
+    }
+    cudaEventRecord(e1, s);
+  }
+  int st = 0;
+  if (!rc) rc = read_int(F->status, &st, s);
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { ooc_set_last_error(e, "mixed factorization", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
+  }
+  float ms = 0;
+  if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) { delete F; return rc; }
+  F->info = st;
+  *info = st;
+  if (stats) {
+    stats->seconds = ms * 1e-3;
+    stats->flops = (double)n * n * n / 3.0;
+    stats->npanels = 1;
+    stats->info = st;
+    stats->kernel_launches = launches;
+  }
+  *out = F;
+  return OOC_OK;
+}
+
+extern "C" int ooc_factor_destroy(ooc_factor* F) {
+  if (!F) return OOC_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(F->device);
+  cudaDeviceSynchronize();
+  delete F;
+  cudaSetDevice(prev);
+  return OOC_OK;
+}
+
+extern "C" int ooc_factor_copy_L(ooc_factor* F, double* L, int64_t ldl) {
+  if (!F) return -1;
+  if (!L) return -2;
+  if (ldl < F->n) return -3;
+  cudaSetDevice(F->device);
+  OOC_CUDA_TRY(cudaMemcpy2D(L, ldl * sizeof(double), F->L, F->n * sizeof(double), F->n * sizeof(double), F->n,
+                            cudaMemcpyDefault));
+  return OOC_OK;
+}
+
+// Plain solve with the factor (FP64 triangular solves): B := A^{-1} B, B on the device.
+extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t ldb, int nrhs) {
+  if (!h) return -1;
+  if (!F) return -2;
+  if (!B) return -3;
+  if (ldb < F->n) return -4;
+  if (nrhs < 0 || nrhs > RMAX) return -5;
+  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+  cudaSetDevice(F->device);
+  cudaStream_t s = ooc_compute_stream(h);
+  int rc = solve_with<double>(F->L, F->n, F->Dinv, F->n, F->nb, B, ldb, nrhs, F->tmp, s, &F->part);
+  if (rc) return rc;
+  return ooc_wait_stream(h, s);
+}
+
+namespace {
+__global__ void k_residual_init(const double* B, i64 ldb, double* R, i64 ldr, int n, int r) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) R[i + q * ldr] = B[i + q * ldb];
+}
+__global__ void k_to_f32_cols(const double* S, i64 lds, float* D, i64 ldd, int n, int r) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) D[i + q * ldd] = (float)S[i + q * lds];
+}
+__global__ void k_add_f32_cols(double* X, i64 ldx, const float* D, i64 ldd, int n, int r) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) X[i + q * ldx] += (double)D[i + q * ldd];
+}
+
+double host_max(const std::vector<double>& v, int r, int q, int nb) {
+  double m = 0;
+  for (int b = 0; b < nb; b++) m = std::max(m, v[(size_t)b * r + q]);
+  return m;
+}
+}  // namespace
+
+// Solve A X = B to a normwise backward error <= tol by iterative refinement with the
+// factor: X0 from the factor in FP64, then repeat R = B - A X (FP64, A the original
+// matrix on the device), D = A_F^{-1} R with the factor (FP32 copy for a reduced-
+// precision factor, FP64 otherwise), X += D.  B, X: device, n x nrhs.  Writes the
+// number of refinement steps and the final backward error (max over columns).
+extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda, const double* B,
+                                int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
+                                double* berr) {
+  if (!h) return -1;
+  if (!F) return -2;
+  if (!A) return -3;
+  if (lda < F->n) return -4;
+  if (!B) return -5;
+  if (ldb < F->n) return -6;
+  if (!X) return -7;
+  if (ldx < F->n) return -8;
+  if (nrhs <= 0 || nrhs > RMAX) return -9;
+  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+  cudaSetDevice(F->device);
+  cudaStream_t s = ooc_compute_stream(h);
+  const i64 n = F->n;
+  const int r = nrhs;
+  double *R = nullptr, *red = nullptr, *rows = nullptr;
+  float* Rf = nullptr;
+  const int nred = 152;
+  if (cudaMalloc(&R, (size_t)n * r * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&red, (size_t)nred * r * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&rows, (size_t)n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&Rf, (size_t)n * r * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    if (R) cudaFree(R);
+    if (red) cudaFree(red);
+    if (rows) cudaFree(rows);
+    return OOC_ERR_NOMEM;
+  }
+  int rc = OOC_OK;
+  std::vector<double> hv((size_t)nred * r), hrow;
+  const unsigned gb = (unsigned)((n + 255) / 256);
+  auto colmax = [&](const double* V, i64 ld, std::vector<double>& out) -> int {
+    k_colmax_abs<<<nred, 256, 0, s>>>(V, ld, (int)n, r, red);
+    OOC_CUDA_TRY(cudaMemcpyAsync(hv.data(), red, hv.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int e = ooc_wait_stream(h, s);
+    if (e) return e;
+    out.assign(r, 0.0);
+    for (int q = 0; q < r; q++) out[q] = host_max(hv, r, q, nred);
+    return OOC_OK;
+  };
+  // ||A||_inf
+  double normA = 0;
+  {
+    k_rowsum_abs<<<gb, 256, 0, s>>>(A, lda, (int)n, rows);
+    std::vector<double> rs(1);
+    k_colmax_abs<<<nred, 256, 0, s>>>(rows, n, (int)n, 1, red);
+    std::vector<double> tmpv(nred);
+    OOC_CUDA_TRY(cudaMemcpyAsync(tmpv.data(), red, nred * sizeof(double), cudaMemcpyDeviceToHost, s));
+    rc = ooc_wait_stream(h, s);
+    for (double v : tmpv) normA = std::max(normA, v);
+  }
+  std::vector<double> nb_(r), nx(r), nr(r);
+  if (!rc) rc = colmax(B, ldb, nb_);
+  // X0 = A_F^{-1} B in FP64
+  if (!rc) {
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
+                                   cudaMemcpyDeviceToDevice, s));
+    rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, X, ldx, r, F->tmp, s, &F->part);
+  }
+  int it = 0;
+  double be = 0;
+  while (!rc) {
+    // R = B - A X (FP64)
+    k_residual_init<<<gb, 256, 0, s>>>(B, ldb, R, n, (int)n, r);
+    rc = gemm_nn_small<double, double>(A, lda, X, ldx, R, n, (int)n, (int)n, r, -1.0, 1.0, s, &F->part);
+    if (rc) break;
+    rc = colmax(R, n, nr);
+    if (rc) break;
+    rc = colmax(X, ldx, nx);
+    if (rc) break;
+    be = 0;
+    for (int q = 0; q < r; q++) {
+      const double den = normA * nx[q] + nb_[q];
+      be = std::max(be, den > 0 ? nr[q] / den : 0.0);
+    }
+    if (be <= tol || it >= maxiter) break;
+    // D = A_F^{-1} R
+    if (F->Lf) {
+      k_to_f32_cols<<<gb, 256, 0, s>>>(R, n, Rf, n, (int)n, r);
+      rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+      if (rc) break;
+      k_add_f32_cols<<<gb, 256, 0, s>>>(X, ldx, Rf, n, (int)n, r);
+    } else {
+      rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, R, n, r, F->tmp, s, &F->part);
+      if (rc) break;
+      k_axpy_cols<<<gb, 256, 0, s>>>(X, ldx, R, n, (int)n, r);
+    }
+    it++;
+  }
+  if (!rc) rc = ooc_wait_stream(h, s);
+  cudaFree(R);
+  cudaFree(red);
+  cudaFree(rows);
+  cudaFree(Rf);
+  if (rc) return rc;
+  if (iters) *iters = it;
+  if (berr) *berr = be;
+  return OOC_OK;
+}
+
+// C (lower, n x n, device) := C - A A^T with A (n x k, device), trailing-update kernels of
+// the given precision.  The dsyrk('L','N', alpha=-1, beta=1) task body of the reference
+// (oocquark.cpp:176), exposed as a tile call.
+extern "C" int ooc_dsyrk_ln(ooc_handle* h, int prec, int n, int k, const double* A, int64_t lda, double* C,
+                            int64_t ldc) {
+  if (!h) return -1;
+  if (prec != OOC_PREC_FP64 && prec != OOC_PREC_FP32 && prec != OOC_PREC_BF16X3) return -2;
+  if (n < 0) return -3;
+  if (k < 0) return -4;
+  if (!A && n > 0) return -5;
+  if (lda < std::max(1, n)) return -6;
+  if (!C && n > 0) return -7;
+  if (ldc < std::max(1, n)) return -8;
+  if (n == 0 || k == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  int* status = nullptr;
+  if (cudaMalloc(&status, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return OOC_ERR_NOMEM; }
+  cudaMemsetAsync(status, 0, sizeof(int), s);
+  DevBuf work;
+  int rc;
+  if (prec == OOC_PREC_FP64) {
+    rc = launch_gemm_nt(A, lda, A, lda, C, ldc, n, n, k, 1, -1.0, status, s);
+  } else {
+    rc = syrk_lowprec(prec, A, lda, C, ldc, n, k, status, s, work);
+  }
+  int st = 0;
+  if (!rc) rc = read_int(status, &st, s);
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { ooc_set_last_error(e, "ooc_dsyrk_ln", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
+  }
+  cudaFree(status);
+  if (rc) return rc;
+  return st == 0 ? OOC_OK : OOC_ERR_TIMEOUT;
+}

@@ -1,0 +1,322 @@
+// Split-BF16 tensor-core trailing update on Blackwell (tcgen05 + TMA + TMEM).
+//
+//   C (FP64, lower triangle) -= X X^T,   X = m x K (FP64, column-major)
+//
+// X is split once per update into BF16 hi/lo planes (x = hi + lo + O(2^-17 |x|)), stored
+// K-major (each row's K values contiguous) so that TMA can stage 128 x 64 tiles with the
+// 128-byte swizzle the tensor core reads.  Each CTA owns one 128 x 128 block of the lower
+// triangle and accumulates, in TMEM (FP32),
+//     D = sum_k  Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T
+// with tcgen05.mma kind::f16 (M=128, N=128, K=16) issued by one thread, fed by a
+// two-stage TMA pipeline (mbarrier complete_tx), then reads D back with tcgen05.ld and
+// subtracts it from the FP64 block (one thread per row, coalesced along columns).
+//
+// Every mbarrier wait is bounded.  A wait that runs out records an error code in the
+// status word (so every later kernel of the factorization returns at once), stops issuing
+// work, waits (bounded) for the MMAs already issued, frees its TMEM and returns.
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int TB = 128;        // output block (rows = cols)
+constexpr int TK = 64;         // K per stage: 64 bf16 = one 128-byte swizzle row
+constexpr int STAGES = 2;
+constexpr int PLANE_BYTES = TB * TK * 2;          // 16 KB: one 128 x 64 bf16 tile
+constexpr int STAGE_BYTES = 4 * PLANE_BYTES;      // Ahi, Alo, Bhi, Blo
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int TMEM_COLS = 128;
+constexpr long long WAIT_LIMIT = 1LL << 22;       // polls before a wait is declared stuck
+constexpr int ERR_TIMEOUT_CODE = -1000003;        // status value written on a stuck wait
+
+// --------------------------------- PTX helpers -----------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// Bounded parity wait: returns true when the phase with `parity` has completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (long long i = 0; i < WAIT_LIMIT; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];\n" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand in 128-byte-swizzled atoms of
+// 8 rows x 128 bytes (stride between atoms 1024 bytes).
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)(16 >> 4) << 16;                   // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                           // fixed 0b001
+  d |= (uint64_t)2 << 61;                           // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: kind::f16 with BF16 A/B, FP32 D, both K-major, M=128, N=128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TB >> 3) << 17) | ((uint32_t)(TB >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// ------------------------------------ kernels ------------------------------------
+// Split: X (m x K FP64, column-major) -> hi/lo planes (Mp x Kp BF16, row-major, zero pad).
+__global__ void k_split_bf16(const double* __restrict__ X, i64 ldx, __nv_bfloat16* __restrict__ hi,
+                             __nv_bfloat16* __restrict__ lo, int m, int K, int Mp, int Kp) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  // read 32 x 32 (rows r0.., cols k0..) coalesced along rows
+  for (int c = threadIdx.y; c < 32; c += blockDim.y) {
+    const int r = r0 + threadIdx.x, k = k0 + c;
+    t[c][threadIdx.x] = (r < m && k < K) ? X[r + (i64)k * ldx] : 0.0;
+  }
+  __syncthreads();
+  // write rows, coalesced along k
+  for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
+    const int r = r0 + rr, k = k0 + threadIdx.x;
+    if (r < Mp && k < Kp) {
+      const double x = t[threadIdx.x][rr];
+      const __nv_bfloat16 h = __double2bfloat16(x);
+      const __nv_bfloat16 l = __double2bfloat16(x - (double)__bfloat162float(h));
+      hi[(i64)r * Kp + k] = h;
+      lo[(i64)r * Kp + k] = l;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_syrk_bf16x3(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+                  double* __restrict__ C, i64 ldc, int m, int Kp, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  int* abort_flag = (int*)(tmem_slot + 1);
+  int* n_issued = abort_flag + 1;    // stages loaded by the producer
+  int* n_consumed = abort_flag + 2;  // stages whose load the MMA thread saw complete
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // lower-triangular block index
+  int bi = (int)((sqrt(8.0 * (double)blockIdx.x + 1.0) - 1.0) * 0.5);
+  while ((bi + 1) * (bi + 2) / 2 <= (int)blockIdx.x) bi++;
+  while (bi * (bi + 1) / 2 > (int)blockIdx.x) bi--;
+  const int bj = blockIdx.x - bi * (bi + 1) / 2;
+  const int m0 = bi * TB, n0 = bj * TB;
+  const int nk = Kp / TK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    *n_issued = 0;
+    *n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    for (int c = 0; c < nk; c++) {
+      const int s = c % STAGES;
+      const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+      if (!mbar_wait(&empty[s], ph ^ 1)) { *(volatile int*)abort_flag = 1; break; }
+      if (*(volatile int*)abort_flag) break;
+      uint8_t* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      tma_load_2d(st + 0 * PLANE_BYTES, &map_hi, &full[s], c * TK, m0);
+      tma_load_2d(st + 1 * PLANE_BYTES, &map_lo, &full[s], c * TK, m0);
+      tma_load_2d(st + 2 * PLANE_BYTES, &map_hi, &full[s], c * TK, n0);
+      tma_load_2d(st + 3 * PLANE_BYTES, &map_lo, &full[s], c * TK, n0);
+      *(volatile int*)n_issued = c + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    int issued = 0;
+    for (int c = 0; c < nk; c++) {
+      const int s = c % STAGES;
+      const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+      if (!mbar_wait(&full[s], ph)) { *(volatile int*)abort_flag = 1; break; }
+      *(volatile int*)n_consumed = c + 1;
+      if (*(volatile int*)abort_flag) break;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+      const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t a_hi = base, a_lo = base + PLANE_BYTES, b_hi = base + 2 * PLANE_BYTES,
+                     b_lo = base + 3 * PLANE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < TK / 16; kk++) {
+        const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
+        const uint32_t acc0 = (c > 0 || kk > 0) ? 1u : 0u;
+        umma_bf16(tmem, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_hi + off), acc0);
+        umma_bf16(tmem, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_lo + off), 1u);
+        umma_bf16(tmem, umma_desc_sw128(a_lo + off), umma_desc_sw128(b_hi + off), 1u);
+      }
+      umma_commit(&empty[s]);  // stage free once these MMAs have read it
+      issued++;
+    }
+    umma_commit(done);  // fires when every MMA issued above has completed
+    (void)issued;
+  }
+  __syncwarp();
+
+  // ---- epilogue: all four warps
+  const bool ok = mbar_wait(done, 0);
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  __syncthreads();
+  if (!ok || *(volatile int*)abort_flag) {
+    if (threadIdx.x == 0) {
+      atomicCAS(status, 0, ERR_TIMEOUT_CODE);
+      // Let loads still in flight land (bounded) before the CTA's shared memory goes away.
+      for (int c = *(volatile int*)n_consumed; c < *(volatile int*)n_issued; c++)
+        (void)mbar_wait(&full[c % STAGES], (uint32_t)((c / STAGES) & 1));
+    }
+  } else {
+    const int row = m0 + warp * 32 + lane;
+    const bool diag = (bi == bj);
+#pragma unroll 1
+    for (int cb = 0; cb < TB; cb += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+            "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+            "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+      if (row < m) {
+#pragma unroll
+        for (int q = 0; q < 32; q++) {
+          const int col = n0 + cb + q;
+          if (col < m && (!diag || col <= row)) {
+            double* p = C + row + (i64)col * ldc;
+            *p -= (double)__uint_as_float(v[q]);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// ------------------------------ host: tensor maps --------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+int get_encode() {
+  std::call_once(g_encode_once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  });
+  return g_encode ? OOC_OK : OOC_ERR_UNSUPPORTED;
+}
+
+int make_map(CUtensorMap* map, void* base, int Mp, int Kp) {
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Mp};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TB};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
+}
+
+}  // namespace
+
+size_t bf16x3_work_bytes(int m, int K) {
+  const size_t Mp = ((size_t)m + TB - 1) / TB * TB;
+  const size_t Kp = ((size_t)K + TK - 1) / TK * TK;
+  return 2 * Mp * Kp * sizeof(__nv_bfloat16) + 256;
+}
+
+int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
+                       void* work, size_t work_bytes) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (!status) return OOC_ERR_INTERNAL;
+  int rc = get_encode();
+  if (rc) return rc;
+  const int Mp = (m + TB - 1) / TB * TB;
+  const int Kp = (K + TK - 1) / TK * TK;
+  if (work_bytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
+  __nv_bfloat16* hi = (__nv_bfloat16*)work;
+  __nv_bfloat16* lo = hi + (size_t)Mp * Kp;
+  dim3 sg((unsigned)(Kp / 32), (unsigned)(Mp / 32));
+  k_split_bf16<<<sg, dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp, Kp);
+  OOC_CUDA_TRY(cudaGetLastError());
+  CUtensorMap mh, ml;
+  if (make_map(&mh, hi, Mp, Kp) || make_map(&ml, lo, Mp, Kp)) {
+    ooc_set_last_message("cuTensorMapEncodeTiled failed for the BF16 split planes");
+    return OOC_ERR_CUDA;
+  }
+  static bool attr = false;
+  if (!attr) {
+    OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr = true;
+  }
+  const i64 T = Mp / TB;
+  const i64 nblk = T * (T + 1) / 2;
+  k_syrk_bf16x3<<<(unsigned)nblk, 128, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, const_cast<int*>(status));
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}

@@ -1,0 +1,145 @@
+"""GPU tests of the mixed-precision factor and the FP64 solve / iterative refinement.
+
+Bars: the plain-precision factor object reproduces the plain path bit for bit; solves
+agree with the oracle's FP64 solve (LAPACK dpotrs on the oracle factor) to a forward
+error of FWD_TOL; refinement reaches the normwise backward error BERR_TOL (1e-14, the
+spec bar) for every precision and every conditioning of the C2 generator.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BERR_TOL = 1e-14
+FWD_TOL = 1e-11
+
+
+def _dev(M):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(M).T)).cuda()
+
+
+def _host(T):
+    return np.asfortranarray(T.cpu().numpy().T)
+
+
+def _c2_matrix(oracle_mod, n, delta, seed=7):
+    alpha = 0.5774 * math.sqrt(n) * (1 + delta)
+    return oracle_mod.gen_uniform(n, seed, alpha), alpha
+
+
+def _berr(A, X, B):
+    R = B - A @ X
+    nA = np.abs(A).sum(axis=1).max()
+    return max(np.abs(R[:, q]).max() / (nA * np.abs(X[:, q]).max() + np.abs(B[:, q]).max()) for q in range(B.shape[1]))
+
+
+def test_fp64_factor_object_matches_plain_path(oracle_mod, handle):
+    n, nb = 1500, 256
+    A = oracle_mod.gen_uniform(n, 3, float(n))
+    T = _dev(A)
+    handle.dpotrf_L(T, n, n, nb, 0)
+    F = handle.factor(_dev(A), n, n, nb, "fp64")
+    assert F.info == 0
+    L = np.asfortranarray(np.empty((n, n)))
+    F.copy_L(L, n)
+    np.testing.assert_array_equal(np.tril(L), np.tril(_host(T)))
+    F.close()
+
+
+@pytest.mark.parametrize("nrhs", [1, 16])
+def test_fp64_solve_matches_oracle(oracle_mod, handle, nrhs):
+    n, nb = 1300, 256
+    A = oracle_mod.gen_uniform(n, 5, float(n))
+    Lo = A.copy(order="F")
+    oracle_mod.cholesky(Lo, nb, 1 << 30, 4, 2)
+    B = np.asfortranarray(np.random.default_rng(2).standard_normal((n, nrhs)))
+    Xo = oracle_mod.potrs(Lo, B)
+    with handle.factor(A, n, n, nb, "fp64") as F:  # host A
+        Bd = _dev(B)
+        F.solve(Bd, n, nrhs)
+        X = _host(Bd)
+    assert np.abs(X - Xo).max() / np.abs(Xo).max() < FWD_TOL
+    assert _berr(A, X, B) < BERR_TOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "bf16x3"])
+@pytest.mark.parametrize("delta", [1.0, 0.1, 0.01])
+@pytest.mark.parametrize("nrhs", [1, 16])
+def test_refinement_reaches_backward_error(oracle_mod, handle, prec, delta, nrhs):
+    n, nb = 2048, 256
+    A, alpha = _c2_matrix(oracle_mod, n, delta)
+    B = np.asfortranarray(np.random.default_rng(11).standard_normal((n, nrhs)))
+    Lo = A.copy(order="F")
+    oracle_mod.cholesky(Lo, nb, 1 << 30, 4, 2)
+    Xo = oracle_mod.potrs(Lo, B)  # the FP64 oracle solve
+    Ad = _dev(A)
+    Bd = _dev(B)
+    import torch
+
+    Xd = torch.empty_like(Bd)
+    with handle.factor(Ad, n, n, nb, prec) as F:
+        assert F.info == 0
+        it, be = F.refine(Ad, n, Bd, n, Xd, n, nrhs, BERR_TOL, 30)
+    X = _host(Xd)
+    assert be <= BERR_TOL, (prec, delta, it, be)
+    assert _berr(A, X, B) <= 2 * BERR_TOL  # recomputed on the host
+    fwd = np.abs(X - Xo).max() / np.abs(Xo).max()
+    assert fwd < FWD_TOL, fwd
+    if prec != "fp64":
+        assert 1 <= it <= 10  # the reduced-precision factor needs (and gets) a few corrections
+
+
+def test_fp32_factor_is_less_accurate_but_close(oracle_mod, handle):
+    # The FP32 trailing updates perturb the factor at FP32 level: its residual is well
+    # above the FP64 factor's, and well below O(1).
+    n, nb = 2048, 256
+    A, alpha = _c2_matrix(oracle_mod, n, 0.1)
+    L64 = np.asfortranarray(np.empty((n, n)))
+    L32 = np.asfortranarray(np.empty((n, n)))
+    with handle.factor(A, n, n, nb, "fp64") as F:
+        F.copy_L(L64, n)
+    with handle.factor(A, n, n, nb, "fp32") as F:
+        F.copy_L(L32, n)
+    L16 = np.asfortranarray(np.empty((n, n)))
+    with handle.factor(A, n, n, nb, "bf16x3") as F:
+        F.copy_L(L16, n)
+    r64 = oracle_mod.residual(L64, "uniform", 7, alpha, tile=256)
+    r32 = oracle_mod.residual(L32, "uniform", 7, alpha, tile=256)
+    r16 = oracle_mod.residual(L16, "uniform", 7, alpha, tile=256)
+    assert r64 < 10 and 1e3 < r32 < 1e10 and 1e3 < r16 < 1e12, (r64, r32, r16)
+
+
+def test_non_spd_factor_refuses_to_solve(oracle_mod, handle, ooc):
+    n, nb = 700, 128
+    A = oracle_mod.gen_uniform(n, 1, float(n))
+    A[400, 400] = -5.0
+    with handle.factor(A, n, n, nb, "fp32") as F:
+        assert F.info == 401
+        import torch
+
+        B = torch.zeros((1, n), dtype=torch.float64, device="cuda")
+        with pytest.raises(ooc.OocError):
+            F.solve(B, n, 1)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-14), ("fp32", 3e-6), ("bf16x3", 1e-4)])
+@pytest.mark.parametrize("n,k", [(1, 64), (100, 64), (128, 128), (129, 100), (300, 512), (1000, 256)])
+def test_dsyrk_kernels_against_fp64(handle, prec, tol, n, k):
+    # C := C - A A^T on the lower triangle; the relative error is measured against the
+    # size of the product, since C itself is an arbitrary offset.
+    rng = np.random.default_rng(n * 1000 + k)
+    A = np.asfortranarray(rng.standard_normal((n, k)))
+    C = np.asfortranarray(rng.standard_normal((n, n)))
+    want = C - A @ A.T
+    Ad, Cd = _dev(A), _dev(C)
+    handle.dsyrk_ln(prec, n, k, Ad, n, Cd, n)
+    got = _host(Cd)
+    lo = np.tril(np.ones((n, n), dtype=bool))
+    scale = np.abs(A @ A.T).max()
+    err = np.abs(got - want)[lo].max() / scale
+    assert err < tol, (prec, n, k, err)
+    np.testing.assert_array_equal(got[~lo], C[~lo])  # strict upper untouched
