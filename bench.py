@@ -1,26 +1,27 @@
-"""Benchmark: out-of-core left-looking FP64 Cholesky on GB300.
+"""Benchmark: out-of-core / mixed-precision Cholesky on GB300.
 
-One JSON line on rank 0 (see the keys below).  A step is one factorization of one
-synthetic SPD matrix A = (R + R^T)/2 + n I (R uniform in [-0.5, 0.5), SplitMix64,
-seed 100 + rank):
+One JSON line on rank 0.  Two forms (``--form``):
 
-* ``value`` -- TFLOP/s (n^3/3 flops) of the factorization with A already resident in
-  HBM (device pointer, factored in place).  Every step first restores A from a
-  pristine device copy (a device-to-device copy inside the timed region; A is larger
-  than L2, so no L2 flush is needed).
-* ``e2e``  -- the same metric through the C-ABI with A in page-locked HOST memory,
-  streamed through a device budget that forces the left-looking out-of-core schedule:
-  every host-to-device panel/column copy and device-to-host copy-back is inside the
-  timed region (byte counts are the library's own).
-* ``roofline`` -- the dominant kernel (the panel update: syrk + gemm on FP64 DMMA),
-  achieved = its algorithmic flops / its CUDA-event time on the launching stream over
-  the timed steps; peak = FP64 DMMA issue rate measured live by the library's probe.
-* ``cpu_baseline`` -- the oracle (a C++ restatement of the reference's QUARK task graph
-  on host BLAS) timed on this host's cores on a bounded sample.
+* ``mixed`` (default; BASELINE configs[2]: n=65536, nb=512, A = (R+R^T)/2 + alpha I with
+  alpha = 0.5774 sqrt(n) (1+delta), delta = 0.1, one N(0,1) right-hand side).  A step is
+  one factorization with split-BF16 tensor-core trailing updates (FP64 diagonal potrf and
+  column solve) followed by FP64 iterative refinement to a normwise backward error
+  <= 1e-14.  ``value`` = n^3/3 / step time with A resident in HBM; ``fp64`` = the same
+  solve done by the plain FP64 path, measured once; the forward and backward errors of
+  every solve are reported per delta.  configs[1] (n=163840, 214.7 GB pinned host matrix)
+  does not fit this machine's host RAM (209 GB in total) and is not run.
+* ``fp64-ooc``: the plain FP64 out-of-core factorization (C1 geometry at n=24576,
+  nb=1024, 1 GiB device budget for the host leg).
 
-``--impl reference`` times the reference algorithm's CPU path (the oracle: QUARK-style
-task graph + host BLAS; the reference itself cannot be built here) on the same
-workload with all host cores.
+Common keys: ``e2e`` is the same metric through the C-ABI with host buffers (page-locked),
+host<->device copies inside the timed region; ``roofline`` reports the dominant kernel
+(achieved from CUDA events on its launching stream over the timed steps, peak from
+MEASURED_PEAKS.json, or the live FP64 DMMA probe for FP64 kernels); ``cpu_baseline`` times
+the oracle (a C++ restatement of the reference's QUARK task graph on host BLAS) on this
+host's cores on a bounded sample.
+
+``--impl reference`` times the reference algorithm's CPU path (the oracle; the reference
+itself cannot be built here) with all host cores on a bounded sample of the workload.
 """
 from __future__ import annotations
 
@@ -52,14 +53,24 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=24576)
-    p.add_argument("--nb", type=int, default=1024)
-    p.add_argument("--budget-mb", type=int, default=1024, help="device panel budget for the e2e (host) leg")
+    p.add_argument("--form", default="mixed", choices=["mixed", "fp64-ooc"])
+    p.add_argument("--n", type=int, default=None)
+    p.add_argument("--nb", type=int, default=None)
+    p.add_argument("--prec", default="bf16x3", choices=["bf16x3", "fp32"])
+    p.add_argument("--delta", type=float, default=0.1)
+    p.add_argument("--nrhs", type=int, default=1)
+    p.add_argument("--budget-mb", type=int, default=1024, help="device panel budget for the fp64-ooc host leg")
     p.add_argument("--seed", type=int, default=100)
     p.add_argument("--cpu-sample-n", type=int, default=12288)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64-ref", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.n is None:
+        a.n = 65536 if a.form == "mixed" else 24576
+    if a.nb is None:
+        a.nb = 512 if a.form == "mixed" else 1024
+    return a
 
 
 # ----------------------------------------------------------------------------------
@@ -171,45 +182,72 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    n, nb = args.n, args.nb
-    budget = args.budget_mb << 20
+    import numpy as np
+
     import oracle
 
     ncores = os.cpu_count() or 1
-    oracle.set_blas_threads(1)
-    for _ in range(args.warmup):
-        A = oracle.gen_uniform(n, args.seed, float(n))
-        oracle.cholesky(A, nb, budget, ncores, 2)
-    total = 0.0
-    for _ in range(args.steps):
-        A = oracle.gen_uniform(n, args.seed, float(n))
-        t, info, npan = oracle.cholesky(A, nb, budget, ncores, 2)
+    oracle.set_blas_threads(1)  # one BLAS thread per task, as the reference links sequential MKL
+    nb = args.nb
+    if args.form == "mixed":
+        # The reference has only the FP64 path: factor (QUARK task graph + host BLAS) and
+        # dpotrs (oocdag.cpp:439), on a bounded sample of the n=65536 workload.
+        n = min(args.n, args.cpu_sample_n)
+        budget = 1 << 40
+        alpha = 0.5774 * (n ** 0.5) * (1 + args.delta)
+        sample = (f"n={n} (of {args.n}), nb={nb}, delta={args.delta}: FP64 factor + dpotrs, the reference's "
+                  f"QUARK task graph restated in C++ on {ncores} host threads, OpenBLAS one thread per task")
+    else:
+        n = args.n
+        budget = args.budget_mb << 20
+        alpha = float(n)
+        sample = (f"full workload n={n}, nb={nb}, budget={args.budget_mb}MiB: the reference's QUARK task graph "
+                  f"restated in C++ on {ncores} host threads, OpenBLAS one thread per task; timer = factorization "
+                  "only (oocdag.cpp:51,90)")
+    rng = np.random.default_rng(args.seed)
+    b = rng.standard_normal((n, args.nrhs))
+
+    def step():
+        A = oracle.gen_uniform(n, args.seed, alpha)
+        t0 = time.perf_counter()
+        t, info, _ = oracle.cholesky(A, nb, budget, ncores, 2)
         if info != 0:
             raise RuntimeError(f"oracle info={info}")
-        total += t
+        if args.form == "mixed":
+            oracle.potrs(A, b)
+        return time.perf_counter() - t0 if args.form == "mixed" else t
+
+    for _ in range(args.warmup):
+        step()
+    total = sum(step() for _ in range(args.steps))
     ms = total / args.steps * 1e3
     val = (n ** 3 / 3.0) / (ms / 1e3) / 1e12
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": f"synthetic: A=(R+R^T)/2+n*I, R~U[-0.5,0.5) SplitMix64 seed {args.seed}",
-        "config": {"workload": f"plain FP64 out-of-core lower Cholesky n={n} nb={nb} budget={args.budget_mb}MiB",
-                   "n": n, "nb": nb, "device_budget_bytes": budget},
-        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": ncores, "kind": "port",
-                         "sample": f"full workload (n={n}), QUARK-style task graph of the reference restated "
-                                   f"in C++ on {ncores} worker threads, host OpenBLAS one thread per task; "
-                                   "timer = factorization only (oocdag.cpp:51,90)"},
+        "data": f"synthetic: A=(R+R^T)/2+alpha*I, R~U[-0.5,0.5) SplitMix64 seed {args.seed}",
+        "config": {"workload": _workload_name(args), "form": args.form, "n": args.n, "nb": nb},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": ncores, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
+def _workload_name(args) -> str:
+    if args.form == "mixed":
+        return (f"configs[2]: mixed-precision ({args.prec} trailing updates, FP64 potrf/trsm) factor + FP64 "
+                f"iterative-refinement solve to backward error <= 1e-14, n={args.n}, nb={args.nb}, "
+                f"delta={args.delta}, nrhs={args.nrhs}")
+    return (f"plain FP64 out-of-core lower Cholesky n={args.n} nb={args.nb} (C1 tile size; e2e: host A, device "
+            f"budget {args.budget_mb} MiB)")
+
+
 # ----------------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------------
-def run_ours(args):
+def run_fp64_ooc(args):
     rank, world, local = dist_env()
     import numpy as np
     import torch
@@ -362,11 +400,241 @@ def run_ours(args):
     return 0
 
 
+def _init_dist():
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def _measured_peaks() -> dict:
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def run_mixed(args):
+    """configs[2]: mixed factor + FP64 refinement, with the plain FP64 solve beside it."""
+    rank, world, local = _init_dist()
+    import numpy as np
+    import torch
+
+    import oocdag_gb300 as ooc
+
+    ooc.load()
+    n, nb, nrhs = args.n, args.nb, args.nrhs
+    seed = args.seed + rank
+    flops = n ** 3 / 3.0
+    alpha = lambda d: 0.5774 * (n ** 0.5) * (1 + d)
+    h = ooc.Handle(local)
+    comp = torch.cuda.ExternalStream(h.stream(0))
+    peaks = _measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    fp64_peak = h.fp64_peak(300.0)
+
+    A = torch.empty((n, n), dtype=torch.float64, device="cuda")  # column-major, ld = n
+    h.matgen_uniform(A, n, n, seed, alpha(args.delta))
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    B = torch.randn((16, n), dtype=torch.float64, device="cuda", generator=g)  # 16 columns of N(0,1)
+    X = torch.empty_like(B)
+    torch.cuda.synchronize()
+
+    def solve(prec, r=nrhs, Amat=A):
+        F = h.factor(Amat, n, n, nb, prec)
+        if F.info != 0:
+            raise RuntimeError(f"info={F.info}")
+        it, be = F.refine(Amat, n, B, n, X, n, r, 1e-14, 30)
+        st = F.stats
+        F.close()
+        return it, be, st
+
+    for _ in range(args.warmup):
+        solve(args.prec)
+    h.set_option(ooc.OPT_PROFILE, 1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(comp)
+    upd_ms = upd_flops = fac_ms = fac_s = 0.0
+    upd_launch = launches = 0
+    iters, berrs = [], []
+    for _ in range(args.steps):
+        it, be, st = solve(args.prec)
+        iters.append(it)
+        berrs.append(be)
+        upd_ms += st["update_ms"]
+        upd_flops += st["update_flops"]
+        upd_launch += st["update_launches"]
+        fac_ms += st["factor_ms"]
+        fac_s += st["seconds"]
+        launches += st["kernel_launches"]
+    e1.record(comp)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    h.set_option(ooc.OPT_PROFILE, 0)
+    ms_local = e0.elapsed_time(e1) / args.steps
+    ms = allreduce_max(ms_local, world)
+    value = flops * world / (ms / 1e3) / 1e12
+
+    # ---- the plain FP64 solve of the same system, measured once ---------------------
+    fp64 = None
+    X64 = None
+    if not args.no_fp64_ref:
+        torch.cuda.synchronize()
+        f0 = time.perf_counter()
+        it64, be64, st64 = solve("fp64")
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - f0
+        X64 = X[:nrhs].clone()
+        fp64 = {"value": flops / t64 / 1e12, "unit": "TFLOP/s", "ms_per_step": t64 * 1e3, "steps": 1,
+                "warmup": 0, "backward_error": be64, "factor_seconds": st64["seconds"],
+                "note": "plain FP64 path (DMMA updates, FP64 solve), same A and b, measured once",
+                "speedup_mixed_over_fp64": (value / world) / (flops / t64 / 1e12)}
+
+    # ---- errors of every solve form, per delta (untimed) --------------------------------
+    errors = []
+    for d in (1.0, 0.1, 0.01):
+        Ad = A if d == args.delta else torch.empty_like(A)
+        if d != args.delta:
+            h.matgen_uniform(Ad, n, n, seed, alpha(d))
+        for r in sorted({1, 16, nrhs}):
+            it, be, _ = solve(args.prec, r, Ad)
+            ent = {"delta": d, "nrhs": r, "iterations": it, "backward_error": be}
+            if d == args.delta and X64 is not None and r <= nrhs:
+                ent["forward_error_vs_fp64"] = float(
+                    ((X[:r] - X64[:r]).abs().max() / X64[:r].abs().max()).item())
+            errors.append(ent)
+        if Ad is not A:
+            del Ad
+    torch.cuda.empty_cache()
+
+    # ---- e2e: host A and b through the C-ABI ------------------------------------------
+    e2e = None
+    if not args.skip_e2e:
+        Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+        Ah.copy_(A)
+        Bh = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+        Bh.copy_(B[:nrhs])
+        Xh = torch.empty_like(Bh)
+        Ad = torch.empty_like(A)
+        Bd = torch.empty((nrhs, n), dtype=torch.float64, device="cuda")
+        Xd = torch.empty_like(Bd)
+
+        def e2e_step():
+            with torch.cuda.stream(comp):
+                Ad.copy_(Ah, non_blocking=True)
+                Bd.copy_(Bh, non_blocking=True)
+            F = h.factor(Ad, n, n, nb, args.prec)
+            F.refine(Ad, n, Bd, n, Xd, n, nrhs, 1e-14, 30)
+            F.close()
+            with torch.cuda.stream(comp):
+                Xh.copy_(Xd, non_blocking=True)
+            comp.synchronize()
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(comp)
+        for _ in range(args.steps):
+            e2e_step()
+        s1.record(comp)
+        torch.cuda.synchronize()
+        e_ms = allreduce_max(s0.elapsed_time(s1) / args.steps, world)
+        e2e = {"value": flops * world / (e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e_ms,
+               "h2d_bytes_per_step": int(n * n * 8 + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8)}
+        del Ah, Bh, Xh, Ad, Bd, Xd
+
+    # ---- roofline of the dominant kernel ------------------------------------------------
+    upd_bytes = 0.0
+    # C lower read + written once per update (16 B per element) plus the FP64 panel read
+    # and the two BF16 planes written and read (12 B per panel element).
+    for j in range(n // nb - 1):
+        m = n - (j + 1) * nb
+        upd_bytes += m * (m + 1) / 2 * 16 + m * nb * (8 + 4 * 2)
+    upd_bytes *= args.steps
+    share_upd = upd_ms / (ms_local * args.steps)
+    share_fac = fac_ms / (ms_local * args.steps)
+    upd_roof = {"kernel": f"k_syrk_{args.prec} (split-BF16 tcgen05 trailing update)" if args.prec == "bf16x3"
+                else "k_syrk_f32 (FP32 trailing update)",
+                "bound": "hbm", "achieved": upd_bytes / (upd_ms / 1e3) / 1e9 if upd_ms else None,
+                "peak": hbm_peak, "unit": "GB/s", "launches": upd_launch,
+                "avg_launch_ms": upd_ms / max(1, upd_launch), "share_of_step": share_upd,
+                "tensor_tflops": 3 * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    if upd_roof["achieved"] and hbm_peak:
+        upd_roof["frac"] = upd_roof["achieved"] / hbm_peak
+    trsm_flops = sum((n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
+    fac_roof = {"kernel": "FP64 diagonal potrf + inverse + column solve (DMMA)", "bound": "fp64-dmma",
+                "achieved": trsm_flops / (fac_ms / 1e3) / 1e12 if fac_ms else None, "peak": fp64_peak,
+                "unit": "TFLOP/s", "share_of_step": share_fac,
+                "peak_source": "measured live: FP64 DMMA issue loop (ooc_fp64_peak_probe)"}
+    if fac_roof["achieved"]:
+        fac_roof["frac"] = fac_roof["achieved"] / fp64_peak
+    dominant, other = (upd_roof, fac_roof) if share_upd >= share_fac else (fac_roof, upd_roof)
+    roofline = dict(dominant)
+    roofline["traffic"] = None
+    roofline["next_kernel"] = other
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        ns_ = min(args.cpu_sample_n, n)
+        oracle.set_blas_threads(1)
+        Ac = oracle.gen_uniform(ns_, seed, 0.5774 * ns_ ** 0.5 * (1 + args.delta))
+        bc = np.random.default_rng(1).standard_normal((ns_, nrhs))
+        c0 = time.perf_counter()
+        _, info, _ = oracle.cholesky(Ac, nb, 1 << 40, os.cpu_count() or 1, 2)
+        oracle.potrs(Ac, bc)
+        tc = time.perf_counter() - c0
+        cpu = {"value": ns_ ** 3 / 3 / tc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"n={ns_} nb={nb}: FP64 factor (the reference's QUARK task graph restated in C++) + "
+                         f"dpotrs, {tc:.1f}s on {os.cpu_count()} host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3+f64" if args.prec == "bf16x3" else "f32+f64",
+            "data": f"synthetic: A=(R+R^T)/2+alpha*I, alpha=0.5774*sqrt(n)*(1+delta), R~U[-0.5,0.5) SplitMix64 "
+                    f"seed {args.seed}+rank; b~N(0,1)",
+            "config": {"workload": _workload_name(args), "form": "mixed", "n": n, "nb": nb, "prec": args.prec,
+                       "delta": args.delta, "nrhs": nrhs, "parallelism": f"replicas x{world}",
+                       "l2": f"inputs larger than L2 ({n * n * 8 / 1e9:.1f} GB)"},
+            "refinement": {"iterations": iters, "backward_error": max(berrs)},
+            "fp64": fp64, "errors": errors,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+            "factor_seconds_avg": fac_s / args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
-    return run_ours(args)
+    if args.form == "mixed":
+        return run_mixed(args)
+    return run_fp64_ooc(args)
 
 
 if __name__ == "__main__":

@@ -140,6 +140,21 @@ int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda,
 int ooc_dsyrk_ln(ooc_handle* h, int prec, int n, int k, const double* A, int64_t lda, double* C,
                  int64_t ldc);
 
+/* ---- batched small systems ---------------------------------------------------- */
+/* Factor and solve `count` SPD systems (orders 1..512) in ONE persistent launch: matrix i
+ * is column-major with ld = n[i] at element offset a_off[i] of A (device; its lower
+ * triangle is replaced by L_i), its right-hand side at b_off[i] of B (device; replaced
+ * by the solution).  info[i] (host) receives LAPACK info; a failed matrix is not solved.
+ * blk_table (host, 16 entries, may be NULL): panel width per size bucket n/32, from
+ * the autotuner.  ctas_per_sm: resident CTAs per SM (0 = occupancy limit).  *seconds:
+ * kernel time.  The per-matrix work restates the reference's tile bodies at small n
+ * (dpotrf oocquark.cpp:87, dtrsm :130, dsyrk/dgemm :176,222) and its dpotrs check
+ * (oocdag.cpp:439).                                                                   */
+int ooc_batched_dposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
+                      double* A, double* B, int* info, const int* blk_table, int ctas_per_sm, double* seconds);
+int ooc_batched_sposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
+                      float* A, float* B, int* info, const int* blk_table, int ctas_per_sm, double* seconds);
+
 /* Size of the device array that ooc_dpotrf_L_static uses as its panel buffer.      */
 #define OOC_STATIC_PANEL_BYTES (64u << 20)
 

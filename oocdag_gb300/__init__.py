@@ -128,6 +128,9 @@ def load(build_if_missing: bool = True):
                                     ctypes.POINTER(OocStats)]
     L.ooc_factor_destroy.argtypes = [P]
     L.ooc_dsyrk_ln.argtypes = [P, I, I, I, P, I64, P, I64]
+    for name in ("ooc_batched_dposv", "ooc_batched_sposv"):
+        getattr(L, name).argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I64), ctypes.POINTER(I64), P, P,
+                                     ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(D)]
     L.ooc_factor_copy_L.argtypes = [P, P, I64]
     L.ooc_factor_solve.argtypes = [P, P, P, I64, I]
     L.ooc_solve_refine.argtypes = [P, P, P, I64, P, I64, P, I64, I, D, I, ctypes.POINTER(I), ctypes.POINTER(D)]
@@ -249,6 +252,25 @@ class Handle:
         """C := C - A A^T (lower) on the device with the given update precision."""
         p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
         _check(load().ooc_dsyrk_ln(self._h, p, n, k, _ptr(A), lda, _ptr(C), ldc), "ooc_dsyrk_ln")
+
+    def batched_posv(self, prec: str, ns, a_off, b_off, A, B, blk_table=None, ctas_per_sm: int = 0):
+        """Factor and solve len(ns) SPD systems in one persistent launch (A, B on the device,
+        matrix i at element offset a_off[i] with ld = ns[i], right-hand side at b_off[i]).
+        prec: 'fp64' or 'fp32' (the storage and arithmetic type of A and B).  Returns
+        (info list, kernel seconds)."""
+        count = len(ns)
+        n_arr = (ctypes.c_int * count)(*[int(x) for x in ns])
+        ao = (ctypes.c_int64 * count)(*[int(x) for x in a_off])
+        bo = (ctypes.c_int64 * count)(*[int(x) for x in b_off])
+        info = (ctypes.c_int * count)()
+        tbl = None
+        if blk_table is not None:
+            tbl = (ctypes.c_int * 16)(*[int(x) for x in blk_table])
+        sec = ctypes.c_double(0)
+        fn = load().ooc_batched_dposv if prec == "fp64" else load().ooc_batched_sposv
+        _check(fn(self._h, count, n_arr, ao, bo, _ptr(A), _ptr(B), info, tbl, ctas_per_sm, ctypes.byref(sec)),
+               "ooc_batched_posv")
+        return list(info), sec.value
 
     def fp64_peak(self, ms: float = 200.0) -> float:
         r = ctypes.c_double()

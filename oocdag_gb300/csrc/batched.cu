@@ -1,0 +1,325 @@
+// Batched factor + solve of many small SPD systems in ONE persistent launch.
+//
+// Thousands of uneven matrices (n in [16, 512]) are too small for the tile pipeline:
+// each would be a handful of tiny launches.  Here every CTA of a persistent grid takes
+// the next matrix from a queue sorted by decreasing size (largest first balances the
+// tail), factors it with a blocked right-looking Cholesky inside the CTA (diagonal block
+// in shared memory, panel solve thread-per-row, trailing update from a shared-memory
+// copy of the panel with 4 x 4 register tiles), then solves for its right-hand side,
+// and moves on.  Per-matrix LAPACK info goes to an array; a failed matrix is skipped.
+// The panel width is chosen per size bucket by the autotuner (oocdag_gb300/autotune.py).
+//
+// The per-tile arithmetic restates the reference's task bodies at small n: the
+// diagonal dpotrf (oocquark.cpp:87), the column dtrsm R/L/T/N (:130) and the
+// dsyrk/dgemm trailing update (:176,222), followed by the dpotrs of its VERIFY block
+// (oocdag.cpp:439).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int BT = 256;        // threads per CTA
+constexpr int NMAX = 512;      // largest matrix order supported
+constexpr int NBUCKETS = 16;   // size buckets of 32: n in [32 q, 32 q + 31]
+
+struct Item {
+  i64 a_off;  // element offset of the matrix (column-major, ld = n)
+  i64 b_off;  // element offset of its right-hand side (overwritten by the solution)
+  int n;
+  int blk;    // panel width for this matrix
+};
+
+template <typename T>
+__device__ __forceinline__ T tsqrt(T x) { return sqrt(x); }
+template <>
+__device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
+
+// Shared layout: D[64][65] (diagonal block), P[NMAX][blk+1] (panel copy).
+template <typename T>
+__device__ int factor_one(T* __restrict__ A, int n, int blk, T* D, T* P, int* s_fail) {
+  const int t = threadIdx.x;
+  const int ldp = blk + 1;
+  for (int k = 0; k < n; k += blk) {
+    const int kb = min(blk, n - k);
+    // 1. diagonal block -> shared, unblocked right-looking Cholesky
+    for (int idx = t; idx < kb * kb; idx += BT) {
+      const int c = idx / kb, r = idx % kb;
+      if (r >= c) D[c * 65 + r] = A[(k + r) + (i64)(k + c) * n];
+    }
+    if (t == 0) *s_fail = 0;
+    __syncthreads();
+    for (int j = 0; j < kb; j++) {
+      if (t == 0) {
+        const T d = D[j * 65 + j];
+        if (!(d > T(0))) *s_fail = k + j + 1;
+        else D[j * 65 + j] = tsqrt(d);
+      }
+      __syncthreads();
+      if (*s_fail) break;
+      const T inv = T(1) / D[j * 65 + j];
+      for (int r = j + 1 + t; r < kb; r += BT) D[j * 65 + r] *= inv;
+      __syncthreads();
+      const int w = kb - j - 1;
+      for (int idx = t; idx < w * w; idx += BT) {
+        const int c = j + 1 + idx / w, r = j + 1 + idx % w;
+        if (r >= c) D[c * 65 + r] -= D[j * 65 + r] * D[j * 65 + c];
+      }
+      __syncthreads();
+    }
+    for (int idx = t; idx < kb * kb; idx += BT) {
+      const int c = idx / kb, r = idx % kb;
+      if (r >= c) A[(k + r) + (i64)(k + c) * n] = D[c * 65 + r];
+    }
+    const int fail = *s_fail;
+    __syncthreads();
+    if (fail) return fail;
+    const int m = n - k - kb;
+    if (m <= 0) break;
+    // 2. panel: rows below, B := B L_kk^-T, one thread per row; result kept in P
+    for (int i = t; i < m; i += BT) {
+      T* row = P + i * ldp;
+      const int gi = k + kb + i;
+      for (int c = 0; c < kb; c++) row[c] = A[gi + (i64)(k + c) * n];
+      for (int c = 0; c < kb; c++) {
+        T v = row[c];
+        for (int q = 0; q < c; q++) v -= row[q] * D[q * 65 + c];
+        v /= D[c * 65 + c];
+        row[c] = v;
+        A[gi + (i64)(k + c) * n] = v;
+      }
+    }
+    __syncthreads();
+    // 3. trailing update of the lower triangle from P (4 x 4 tiles per thread)
+    const int Tt = (m + 3) / 4;
+    const int ntile = Tt * (Tt + 1) / 2;
+    for (int tile = t; tile < ntile; tile += BT) {
+      int ti = (int)((sqrtf(8.f * (float)tile + 1.f) - 1.f) * 0.5f);
+      while ((ti + 1) * (ti + 2) / 2 <= tile) ti++;
+      while (ti * (ti + 1) / 2 > tile) ti--;
+      const int tj = tile - ti * (ti + 1) / 2;
+      T acc[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+      const int r0 = ti * 4, c0 = tj * 4;
+      for (int q = 0; q < kb; q++) {
+        T ra[4], cb[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) ra[a] = (r0 + a < m) ? P[(r0 + a) * ldp + q] : T(0);
+#pragma unroll
+        for (int b = 0; b < 4; b++) cb[b] = (c0 + b < m) ? P[(c0 + b) * ldp + q] : T(0);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int b = 0; b < 4; b++) acc[a][b] = fma(ra[a], cb[b], acc[a][b]);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const int r = r0 + a, c = c0 + b;
+          if (r < m && c < m && c <= r) {
+            T* p = A + (k + kb + r) + (i64)(k + kb + c) * n;
+            *p -= acc[a][b];
+          }
+        }
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
+// L L^T x = b in place (b in global), blocks of 32 rows: one warp solves the diagonal
+// block with shuffles, all threads update the rest.
+template <typename T>
+__device__ void solve_one(const T* __restrict__ L, int n, T* __restrict__ b) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  // forward
+  for (int k = 0; k < n; k += 32) {
+    const int kb = min(32, n - k);
+    if (warp == 0) {
+      T v = (lane < kb) ? b[k + lane] : T(0);
+      for (int j = 0; j < kb; j++) {
+        T yj = __shfl_sync(0xffffffffu, v, j);
+        if (lane == j) { yj = v / L[(k + j) + (i64)(k + j) * n]; v = yj; }
+        yj = __shfl_sync(0xffffffffu, v, j);
+        if (lane > j && lane < kb) v -= L[(k + lane) + (i64)(k + j) * n] * yj;
+      }
+      if (lane < kb) b[k + lane] = v;
+    }
+    __syncthreads();
+    for (int i = k + kb + t; i < n; i += BT) {
+      T s = T(0);
+      for (int j = 0; j < kb; j++) s = fma(L[i + (i64)(k + j) * n], b[k + j], s);
+      b[i] -= s;
+    }
+    __syncthreads();
+  }
+  // backward: L^T x = y
+  for (int k = ((n - 1) / 32) * 32; k >= 0; k -= 32) {
+    const int kb = min(32, n - k);
+    if (warp == 0) {
+      T v = (lane < kb) ? b[k + lane] : T(0);
+      for (int j = kb - 1; j >= 0; j--) {
+        T xj = __shfl_sync(0xffffffffu, v, j);
+        if (lane == j) { xj = v / L[(k + j) + (i64)(k + j) * n]; v = xj; }
+        xj = __shfl_sync(0xffffffffu, v, j);
+        if (lane < j) v -= L[(k + j) + (i64)(k + lane) * n] * xj;  // (L^T)(lane, j) = L(j, lane)
+      }
+      if (lane < kb) b[k + lane] = v;
+    }
+    __syncthreads();
+    for (int i = t; i < k; i += BT) {
+      T s = T(0);
+      for (int j = 0; j < kb; j++) s = fma(L[(k + j) + (i64)i * n], b[k + j], s);
+      b[i] -= s;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ items, int count, T* A, T* B,
+                                                     int* info, int* counter, int do_solve) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  T* D = (T*)smem_raw;
+  T* P = D + 64 * 65;
+  __shared__ int s_idx, s_fail;
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1);
+    __syncthreads();
+    const int idx = s_idx;
+    __syncthreads();
+    if (idx >= count) break;
+    const Item it = items[idx];
+    const int f = factor_one<T>(A + it.a_off, it.n, it.blk, D, P, &s_fail);
+    if (threadIdx.x == 0) info[idx] = f;
+    if (f == 0 && do_solve) solve_one<T>(A + it.a_off, it.n, B + it.b_off);
+    __syncthreads();
+  }
+}
+
+// Scatter per-matrix info from sorted order back to the caller's order.
+__global__ void k_scatter_info(const int* sorted_info, const int* order, int count, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[order[i]] = sorted_info[i];
+}
+
+template <typename T>
+size_t smem_for(int blk) { return (size_t)(64 * 65 + NMAX * (blk + 1)) * sizeof(T); }
+
+template <typename T>
+int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off, T* A, T* B,
+                int* info_host, const int* blk_table, int ctas_per_sm, int do_solve, double* seconds) {
+  cudaStream_t s = ooc_compute_stream(h);
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  std::vector<Item> items(count);
+  int maxblk = 1;
+  for (int i = 0; i < count; i++) {
+    const int j = order[i];
+    const int bucket = std::min(NBUCKETS - 1, n[j] / 32);
+    int blk = blk_table ? blk_table[bucket] : (sizeof(T) == 8 ? 32 : 64);
+    blk = std::max(1, std::min(blk, sizeof(T) == 8 ? 32 : 64));
+    items[i] = Item{a_off[j], b_off[j], n[j], blk};
+    maxblk = std::max(maxblk, blk);
+  }
+  Item* d_items = nullptr;
+  int *d_info = nullptr, *d_order = nullptr, *d_out = nullptr, *d_counter = nullptr;
+  int rc = OOC_OK;
+  if (cudaMalloc(&d_items, sizeof(Item) * count) != cudaSuccess || cudaMalloc(&d_info, sizeof(int) * count) != cudaSuccess ||
+      cudaMalloc(&d_order, sizeof(int) * count) != cudaSuccess || cudaMalloc(&d_out, sizeof(int) * count) != cudaSuccess ||
+      cudaMalloc(&d_counter, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    rc = OOC_ERR_NOMEM;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!rc) {
+    cudaMemcpyAsync(d_items, items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+    const size_t sm = smem_for<T>(maxblk);
+    if (cudaFuncSetAttribute(k_batched_posv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
+      cudaGetLastError();
+      rc = OOC_ERR_UNSUPPORTED;
+    } else {
+      int dev = ooc_device(h), nsm = 0;
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      int occ = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_posv<T>, BT, sm);
+      const int per = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : occ, std::max(occ, 1)));
+      const int grid = std::max(1, std::min(count, nsm * per));
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, s);
+      k_batched_posv<T><<<grid, BT, sm, s>>>(d_items, count, A, B, d_info, d_counter, do_solve);
+      cudaEventRecord(e1, s);
+      k_scatter_info<<<(count + 255) / 256, 256, 0, s>>>(d_info, d_order, count, d_out);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) { ooc_set_last_error(e, "k_batched_posv", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
+    }
+  }
+  if (!rc) {
+    cudaMemcpyAsync(info_host, d_out, sizeof(int) * count, cudaMemcpyDeviceToHost, s);
+    rc = ooc_wait_stream(h, s);
+  }
+  if (!rc && seconds) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *seconds = ms * 1e-3;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d_items);
+  cudaFree(d_info);
+  cudaFree(d_order);
+  cudaFree(d_out);
+  cudaFree(d_counter);
+  return rc;
+}
+
+template <typename T>
+int check_args(int count, const int* n, const int64_t* a_off, const int64_t* b_off, const T* A, const T* B,
+               int* info) {
+  if (count < 0) return -3;
+  if (count > 0 && (!n || !a_off || !b_off)) return -4;
+  if (count > 0 && (!A || !B)) return -7;
+  if (!info && count > 0) return -9;
+  for (int i = 0; i < count; i++)
+    if (n[i] < 1 || n[i] > NMAX) return -4;
+  return OOC_OK;
+}
+
+}  // namespace
+
+extern "C" int ooc_batched_dposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
+                                 double* A, double* B, int* info, const int* blk_table, int ctas_per_sm,
+                                 double* seconds) {
+  if (!h) return -1;
+  int rc = check_args<double>(count, n, a_off, b_off, A, B, info);
+  if (rc) return rc;
+  if (count == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  return run_batched<double>(h, count, n, a_off, b_off, A, B, info, blk_table, ctas_per_sm, 1, seconds);
+}
+
+extern "C" int ooc_batched_sposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
+                                 float* A, float* B, int* info, const int* blk_table, int ctas_per_sm,
+                                 double* seconds) {
+  if (!h) return -1;
+  int rc = check_args<float>(count, n, a_off, b_off, A, B, info);
+  if (rc) return rc;
+  if (count == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  return run_batched<float>(h, count, n, a_off, b_off, A, B, info, blk_table, ctas_per_sm, 1, seconds);
+}

@@ -68,6 +68,11 @@ int launch_panel_update(const TileCol& X, const TileMap& C, int Ht, int Kt, i64 
 int launch_gemm_nt(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m,
                    int n, int k, int lower, double alpha, const int* status, cudaStream_t s);
 
+// C[m x n] += alpha * A[m x k] * B[n x k]^T with B lower triangular (B(j, kk) = 0 for
+// kk > j): the zero part of K is skipped, so a triangular product costs its own flops.
+int launch_gemm_nt_trib(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m, int n, int k,
+                        double alpha, const int* status, cudaStream_t s);
+
 // Lower Cholesky of an n x n tile in place (leading dimension ld).  On failure writes
 // status = col0 + (1-based local column) unless status is already non-zero.
 int launch_potrf_tile(double* A, i64 ld, int n, i64 col0, int* status, cudaStream_t s);

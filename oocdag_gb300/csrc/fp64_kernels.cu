@@ -123,20 +123,27 @@ __device__ __forceinline__ void gemm_block(const double* __restrict__ A, i64 lda
     __syncthreads();
   }
 
+  // Epilogue, one 8-row group at a time: its loads of C first, then its stores (a load
+  // after a store to a possibly aliasing address would wait for memory each time).
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int r = m0 + wm * 32 + i * 8 + g;
-    if (r >= m) continue;
+    double cv[4][2];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < 4; j++)
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const int c = n0 + wn * 32 + j * 8 + 2 * tig + h;
-        if (c >= n || (lower && c > r)) continue;
-        double* p = C + r + (i64)c * ldc;
-        *p = fma(alpha, acc[i][j][h], *p);
+        const bool ok = r < m && c < n && !(lower && c > r);
+        cv[j][h] = ok ? C[r + (i64)c * ldc] : 0.0;
       }
-    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int c = n0 + wn * 32 + j * 8 + 2 * tig + h;
+        if (r < m && c < n && !(lower && c > r)) C[r + (i64)c * ldc] = fma(alpha, acc[i][j][h], cv[j][h]);
+      }
   }
 }
 
@@ -178,6 +185,7 @@ struct GemmBatch {
   double* C; i64 ldc, sC;
   int m, m_last, n, k, lower, batch;
   double alpha;
+  int tri_b;  // B lower triangular (B(j, kk) = 0 for kk > j): skip the zero K range
 };
 
 template <bool VEC>
@@ -190,8 +198,9 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_gemm_batched(GemmBatch gb, con
   const int n0 = (blockIdx.x / mblocks) * BN;
   if (m0 >= m || n0 >= gb.n) return;
   if (gb.lower && n0 > m0 + BM - 1) return;
+  const int kmax = gb.tri_b ? min(gb.k, n0 + BN) : gb.k;
   gemm_block<VEC>(gb.A + (i64)z * gb.sA, gb.lda, gb.B + (i64)z * gb.sB, gb.ldb,
-                  gb.C + (i64)z * gb.sC, gb.ldc, m, gb.n, gb.k, m0, n0, gb.lower, gb.alpha);
+                  gb.C + (i64)z * gb.sC, gb.ldc, m, gb.n, kmax, m0, n0, gb.lower, gb.alpha);
 }
 
 // ---------------------------------------------------------------------------------
@@ -319,7 +328,13 @@ static int launch_gemm_batched(const GemmBatch& gb, const int* status, cudaStrea
 
 int launch_gemm_nt(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m, int n,
                    int k, int lower, double alpha, const int* status, cudaStream_t s) {
-  GemmBatch gb{A, lda, 0, B, ldb, 0, C, ldc, 0, m, m, n, k, lower, 1, alpha};
+  GemmBatch gb{A, lda, 0, B, ldb, 0, C, ldc, 0, m, m, n, k, lower, 1, alpha, 0};
+  return launch_gemm_batched(gb, status, s);
+}
+
+int launch_gemm_nt_trib(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, int m, int n, int k,
+                        double alpha, const int* status, cudaStream_t s) {
+  GemmBatch gb{A, lda, 0, B, ldb, 0, C, ldc, 0, m, m, n, k, 0, 1, alpha, 1};
   return launch_gemm_batched(gb, status, s);
 }
 
@@ -375,7 +390,7 @@ int launch_trsm_col(const double* L, i64 ldl, const TileCol& B, int ntiles, int 
       GemmBatch gb{Bb + (i64)k * B.ld, B.ld, B.stride,
                    L + (k + kb) + (i64)k * ldl, ldl, 0,
                    Bb + (i64)(k + kb) * B.ld, B.ld, B.stride,
-                   nb, m_last, rest, kb, 0, ntiles, -1.0};
+                   nb, m_last, rest, kb, 0, ntiles, -1.0, 0};
       rc = launch_gemm_batched(gb, status, s);
       if (rc) return rc;
     }

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
   // quarters 2/3 the same shifted by 64.
   float* stage = smem;
   const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
   for (int qtr = 0; qtr < 4; qtr++) {
     const int half = qtr >> 1;      // which group of 4 accumulator columns
     const int lo_tx = (qtr & 1) * 8;  // threads whose columns fall in this quarter
@@ -124,16 +125,23 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
       }
     }
     __syncthreads();
-    for (int cc = warp; cc < 32; cc += FTHR / 32) {
+    // each warp: 4 columns x 128 rows; all loads before the stores
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int cc = warp * 4 + u;
       const int c = n0 + half * 64 + (qtr & 1) * 32 + cc;
-      if (c >= m) continue;
+      double cv[4];
+      bool ok[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int r = m0 + lane + 32 * q;
+        ok[q] = (c < m) && (r < m) && !(bi == bj && c > r);
+        cv[q] = ok[q] ? C[r + (i64)c * ldc] : 0.0;
+      }
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int rr = lane + 32 * q;
-        const int r = m0 + rr;
-        if (r >= m || (bi == bj && c > r)) continue;
-        double* p = C + r + (i64)c * ldc;
-        *p -= (double)stage[cc * 129 + rr];
+        if (ok[q]) C[m0 + rr + (i64)c * ldc] = cv[q] - (double)stage[cc * 129 + rr];
       }
     }
     __syncthreads();
@@ -248,6 +256,21 @@ __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A,
   for (int q = 0; q < r; q++) {
     TC* c = C + row + (i64)q * ldc;
     *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
+  }
+}
+
+// D (n x n, ld ldd) -> E = D^T (ld lde).
+__global__ void k_transpose(const double* __restrict__ D, i64 ldd, double* __restrict__ E, i64 lde, int n) {
+  __shared__ double t[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int r = bx + threadIdx.x, c = by + yy;
+    t[yy][threadIdx.x] = (r < n && c < n) ? D[r + (i64)c * ldd] : 0.0;
+  }
+  __syncthreads();
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    const int r = by + threadIdx.x, c = bx + yy;  // E(r, c) = D(c, r)
+    if (r < n && c < n) E[r + (i64)c * lde] = t[threadIdx.x][yy];
   }
 }
 
@@ -458,7 +481,7 @@ struct ooc_factor {
   float* tmpf = nullptr;
   int* status = nullptr;   // device status word of the factorization
   int info = 0;
-  DevBuf part, partf, work;
+  DevBuf part, partf, work, scratch;
   ~ooc_factor() {
     if (L) cudaFree(L);
     if (Dinv) cudaFree(Dinv);
@@ -493,53 +516,78 @@ int alloc_factor(ooc_factor* F, i64 n, int nb, bool want_f32) {
   return OOC_OK;
 }
 
-// Diagonal-tile inverses: Dinv_J = I * L_JJ^{-T} through the FP64 column solve.
-int diag_inverses(ooc_factor* F, cudaStream_t s) {
-  const int nb = F->nb;
-  const int bb = (int)((F->n + nb - 1) / nb);
-  const i64 tile = (i64)nb * nb;
-  for (int J = 0; J < bb; J++) {
-    const int LN = (int)std::min<i64>(nb, F->n - (i64)J * nb);
-    double* D = F->Dinv + (i64)J * tile;
-    k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s>>>(D, nb, LN);
-    const double* LJJ = F->L + (i64)J * nb * (1 + F->n);
-    int rc = launch_trsm_col(LJJ, F->n, TileCol{D, nb, tile}, 1, LN, LN, LN, F->status, s);
-    if (rc) return rc;
-  }
-  OOC_CUDA_TRY(cudaGetLastError());
-  return OOC_OK;
-}
-
-// Right-looking in-core factorization of F->L (ld n) with FP64 potrf/trsm and trailing
-// updates in `prec` (the reference's ooc_incore over the whole matrix,
+// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and column solve and
+// trailing updates in `prec` (the reference's ooc_incore over the whole matrix,
 // oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-triangular update).
-int factor_mixed(ooc_factor* F, int prec, cudaStream_t s, int64_t* launches) {
+// The column solve B := B L_jj^{-T} runs as one FP64 DMMA product with the tile's
+// inverse, B := W (L_jj^{-1})^T with W a copy of B, after the inverse (kept for the solves)
+// is formed from the diagonal tile alone; the triangular structure of L_jj^{-1} is
+// skipped in K, so the product costs the solve's own flops but runs as one parallel launch.
+struct MixedProf {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;  // pairs: [2k] start, [2k+1] end
+  std::vector<int> kind;        // 0 = FP64 factor + column solve, 1 = trailing update
+  std::vector<double> flops;    // algorithmic flops of each update
+  cudaEvent_t mark(cudaStream_t s) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+    return e;
+  }
+  ~MixedProf() { for (cudaEvent_t e : ev) cudaEventDestroy(e); }
+};
+
+int factor_mixed(ooc_factor* F, int prec, cudaStream_t s, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
   const int bb = (int)((n + nb - 1) / nb);
   double* A = F->L;
   const i64 lda = n;
+  const i64 tile = (i64)nb * nb;
+  int rc = F->scratch.ensure((size_t)n * nb * sizeof(double) + (size_t)tile * sizeof(double));
+  if (rc) return rc;
+  double* W = (double*)F->scratch.p;   // copy of the column panel (m x nb, ld n)
+  double* E = W + (size_t)n * nb;      // L_jj^{-1} (lower, ld nb)
   for (int j = 0; j < bb; j++) {
     const i64 J0 = (i64)j * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
     double* Djj = A + J0 + J0 * lda;
-    int rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s);
+    if (prof->on) { prof->mark(s); prof->kind.push_back(0); }
+    rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s);
     if (rc) return rc;
-    const int below = bb - j - 1;
-    if (below > 0) {
-      const int m_last = (int)(n - (i64)(bb - 1) * nb);
-      rc = launch_trsm_col(Djj, lda, TileCol{Djj + LN, lda, nb}, below, nb, m_last, LN, F->status, s);
+    // Dinv_j = I L_jj^{-T} = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
+    double* Dj = F->Dinv + (i64)j * tile;
+    k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s>>>(Dj, nb, LN);
+    rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s);
+    if (rc) return rc;
+    k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s>>>(Dj, nb, E, nb, LN);
+    const i64 m = n - J0 - LN;
+    if (m > 0) {
+      double* Pn = Djj + LN;  // the panel below the diagonal tile
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(W, n * sizeof(double), Pn, lda * sizeof(double), m * sizeof(double), LN,
+                                     cudaMemcpyDeviceToDevice, s));
+      OOC_CUDA_TRY(cudaMemset2DAsync(Pn, lda * sizeof(double), 0, m * sizeof(double), LN, s));
+      rc = launch_gemm_nt_trib(W, n, E, nb, Pn, lda, (int)m, LN, LN, 1.0, F->status, s);
       if (rc) return rc;
-      const i64 m = n - J0 - LN;
+      if (prof->on) {
+        prof->mark(s);
+        prof->mark(s);
+        prof->kind.push_back(1);
+        prof->flops.push_back((double)m * (double)(m + 1) * LN);
+      }
       if (prec == OOC_PREC_FP64) {
-        TileMap C{A + (J0 + LN) * (1 + lda), lda, 0, below, nb};
-        rc = launch_panel_update(TileCol{Djj + LN, lda, nb}, C, below, below, m, m, LN, F->status, s);
+        TileMap C{A + (J0 + LN) * (1 + lda), lda, 0, bb - j - 1, nb};
+        rc = launch_panel_update(TileCol{Pn, lda, nb}, C, bb - j - 1, bb - j - 1, m, m, LN, F->status, s);
       } else {
-        rc = syrk_lowprec(prec, Djj + LN, lda, A + (J0 + LN) * (1 + lda), lda, (int)m, LN, F->status, s, F->work);
+        rc = syrk_lowprec(prec, Pn, lda, A + (J0 + LN) * (1 + lda), lda, (int)m, LN, F->status, s, F->work);
       }
       if (rc) return rc;
+      if (prof->on) prof->mark(s);
+    } else if (prof->on) {
+      prof->mark(s);
     }
-    if (launches) *launches += 6 * ((LN + 63) / 64) + 2;
+    if (launches) *launches += 3 * ((LN + 63) / 64) + 2 * ((LN + 63) / 64) + 5;
   }
   return OOC_OK;
 }
@@ -585,10 +633,15 @@ extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int6
     rc = OOC_ERR_CUDA;
   }
   int64_t launches = 0;
+  MixedProf prof;
+  {
+    int64_t pv = 0;
+    ooc_get_option(h, OOC_OPT_PROFILE, &pv);
+    prof.on = pv != 0;
+  }
   if (!rc) {
     cudaEventRecord(e0, s);
-    rc = factor_mixed(F, prec, s, &launches);
-    if (!rc) rc = diag_inverses(F, s);
+    rc = factor_mixed(F, prec, s, &launches, &prof);
     if (!rc && F->Lf) {
       const int bb = (int)((n + nb - 1) / nb);
       k_copy_conv<double, float><<<dim3((unsigned)((n + 255) / 256), 1024), 256, 0, s>>>(F->L, n, F->Lf, n, (int)n,
@@ -617,6 +670,15 @@ extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int6
     stats->npanels = 1;
     stats->info = st;
     stats->kernel_launches = launches;
+    if (prof.on) {
+      size_t fi = 0;
+      for (size_t k = 0; k < prof.kind.size(); k++) {
+        float t = 0;
+        cudaEventElapsedTime(&t, prof.ev[2 * k], prof.ev[2 * k + 1]);
+        if (prof.kind[k] == 0) stats->factor_ms += t;
+        else { stats->update_ms += t; stats->update_launches++; stats->update_flops += prof.flops[fi++]; }
+      }
+    }
   }
   *out = F;
   return OOC_OK;

@@ -238,13 +238,19 @@ __global__ void __launch_bounds__(128, 1)
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
       if (row < m) {
+        // All 32 loads first, then the stores: interleaved load/store pairs to possibly
+        // aliasing addresses would serialize on memory latency.
+        double* base = C + row + (i64)(n0 + cb) * ldc;
+        double cv[32];
 #pragma unroll
         for (int q = 0; q < 32; q++) {
           const int col = n0 + cb + q;
-          if (col < m && (!diag || col <= row)) {
-            double* p = C + row + (i64)col * ldc;
-            *p -= (double)__uint_as_float(v[q]);
-          }
+          cv[q] = (col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 32; q++) {
+          const int col = n0 + cb + q;
+          if (col < m && (!diag || col <= row)) base[(i64)q * ldc] = cv[q] - (double)__uint_as_float(v[q]);
         }
       }
     }
