@@ -134,6 +134,21 @@ int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda,
                      int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
                      double* berr);
 
+/* The same for the uniform test matrix A = (R + R^T)/2 + alpha I of seed `seed`
+ * (ooc_dmatgen_uniform), generated straight into the factor's storage: no copy of A is
+ * kept.  The refinement below regenerates A's elements inside its FP64 residual, so a
+ * seeded system needs only the factor's memory (8 n^2 bytes, 12 n^2 for a reduced-
+ * precision factor).                                                                 */
+int ooc_factor_create_gen(ooc_handle* h, int64_t n, uint64_t seed, double alpha, int nb, int prec,
+                          ooc_factor** F, int* info, ooc_stats* stats);
+int ooc_solve_refine_gen(ooc_handle* h, ooc_factor* F, uint64_t seed, double alpha, const double* B,
+                         int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
+                         double* berr);
+/* Device bytes a factor object of order n, tile nb and precision prec holds.         */
+int64_t ooc_factor_bytes(int64_t n, int nb, int prec);
+/* B (n x nrhs, device) := N(0,1) samples of stream `seed` (Box-Muller on SplitMix64).  */
+int ooc_gen_normal(ooc_handle* h, double* B, int64_t n, int64_t ldb, int nrhs, uint64_t seed);
+
 /* C := C - A A^T on the lower triangle (device pointers; A n x k), with the trailing-
  * update kernel of precision `prec`: the dsyrk('L','N',-1,A,1,C) task body of the
  * reference (oocquark.cpp:176, cublasDsyrk_v2) as a tile call.                       */
@@ -154,6 +169,55 @@ int ooc_batched_dposv(ooc_handle* h, int count, const int* n, const int64_t* a_o
                       double* A, double* B, int* info, const int* blk_table, int ctas_per_sm, double* seconds);
 int ooc_batched_sposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
                       float* A, float* B, int* info, const int* blk_table, int ctas_per_sm, double* seconds);
+
+/* ---- serving: continuous batching of factor + solve requests ------------------- */
+/* A request loop with no counterpart in the reference (which factors one matrix per
+ * process).  Requests are admitted in arrival order against a device-memory budget
+ * (least-recently-used resident factors are evicted when nobody uses them); systems with
+ * n <= small_max_n are gathered by a batcher into one persistent batched launch, larger
+ * ones run on `workers` concurrent pipelines (own streams each) as a factor with
+ * trailing updates in `prec` plus FP64 refinement to `tol`; factors stay resident under
+ * the request's key for repeat solves.  Matrices are the uniform test matrices
+ * (R + R^T)/2 + n I of the request's seed, right-hand sides N(0,1) of its rhs seed.    */
+typedef struct ooc_server ooc_server;
+typedef struct ooc_server_config {
+  int device;
+  int workers;             /* concurrent pipelines for the larger systems (default 4)     */
+  int small_max_n;         /* n <= this goes to the batched kernel (<= 512, default 512)  */
+  int nb;                  /* tile size of the larger systems (default 512)              */
+  int prec;                /* OOC_PREC_* of their trailing updates                       */
+  double tol;              /* backward-error target (default 1e-14)                      */
+  double batch_window_ms;  /* the batcher waits this long for more small requests        */
+  int64_t hbm_budget;      /* device bytes the server may hold (0 = 90% of free memory)  */
+} ooc_server_config;
+typedef struct ooc_request {
+  int kind;                /* 0: factor + solve, 1: solve with the factor resident under key */
+  int64_t n;
+  uint64_t matrix_seed;
+  uint64_t rhs_seed;
+  int64_t key;
+  int keep_solution;       /* 1: keep x until ooc_server_solution fetches it             */
+} ooc_request;
+typedef struct ooc_completion {
+  int64_t id;
+  int status;              /* OOC_OK or an error (OOC_ERR_BUDGET: never fits the budget) */
+  int info;                /* LAPACK info                                                 */
+  int path;                /* 0: batched kernel, 1: factor + refinement pipeline          */
+  int factor_reused;       /* 1: solved with a resident factor                            */
+  int iterations;          /* refinement steps                                            */
+  double backward_error;   /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)           */
+  double t_submit, t_admit, t_done;  /* seconds on the server clock                       */
+  double x_sum;            /* sum of the solution's entries                               */
+} ooc_completion;
+int ooc_server_create(const ooc_server_config* cfg, ooc_server** s);
+int ooc_server_submit(ooc_server* s, const ooc_request* r, int64_t* id);
+/* Up to `max` completions; waits up to wait_ms for the first one.                    */
+int ooc_server_poll(ooc_server* s, ooc_completion* out, int max, int* count, int wait_ms);
+int ooc_server_solution(ooc_server* s, int64_t id, double* x, int64_t n);
+int ooc_server_status(ooc_server* s, int64_t* pending, int64_t* running, int64_t* resident_bytes,
+                      int64_t* reserved_bytes);
+double ooc_server_now(ooc_server* s);
+int ooc_server_destroy(ooc_server* s);
 
 /* Size of the device array that ooc_dpotrf_L_static uses as its panel buffer.      */
 #define OOC_STATIC_PANEL_BYTES (64u << 20)

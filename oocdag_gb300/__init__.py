@@ -128,6 +128,12 @@ def load(build_if_missing: bool = True):
                                     ctypes.POINTER(OocStats)]
     L.ooc_factor_destroy.argtypes = [P]
     L.ooc_dsyrk_ln.argtypes = [P, I, I, I, P, I64, P, I64]
+    L.ooc_factor_create_gen.argtypes = [P, I64, U64, D, I, I, ctypes.POINTER(P), ctypes.POINTER(I),
+                                        ctypes.POINTER(OocStats)]
+    L.ooc_solve_refine_gen.argtypes = [P, P, U64, D, P, I64, P, I64, I, D, I, ctypes.POINTER(I), ctypes.POINTER(D)]
+    L.ooc_factor_bytes.argtypes = [I64, I, I]
+    L.ooc_factor_bytes.restype = I64
+    L.ooc_gen_normal.argtypes = [P, P, I64, I64, I, U64]
     for name in ("ooc_batched_dposv", "ooc_batched_sposv"):
         getattr(L, name).argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I64), ctypes.POINTER(I64), P, P,
                                      ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(D)]
@@ -248,6 +254,21 @@ class Handle:
                                         ctypes.byref(st)), "ooc_factor_create")
         return Factor(self, F, n, info.value, st.as_dict())
 
+    def factor_gen(self, n: int, seed: int, alpha: float, nb: int, prec="bf16x3") -> "Factor":
+        """Factor the uniform test matrix of `seed` generated in place (no copy of A kept)."""
+        p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+        F = ctypes.c_void_p()
+        info = ctypes.c_int(0)
+        st = OocStats()
+        _check(load().ooc_factor_create_gen(self._h, n, seed, float(alpha), nb, p, ctypes.byref(F),
+                                            ctypes.byref(info), ctypes.byref(st)), "ooc_factor_create_gen")
+        f = Factor(self, F, n, info.value, st.as_dict())
+        f.gen = (seed, float(alpha))
+        return f
+
+    def gen_normal(self, B, n: int, ldb: int, nrhs: int, seed: int) -> None:
+        _check(load().ooc_gen_normal(self._h, _ptr(B), n, ldb, nrhs, seed), "ooc_gen_normal")
+
     def dsyrk_ln(self, prec, n: int, k: int, A, lda: int, C, ldc: int) -> None:
         """C := C - A A^T (lower) on the device with the given update precision."""
         p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
@@ -316,6 +337,7 @@ class Factor:
     """A factor kept on the device for repeated solves (ooc_factor)."""
 
     def __init__(self, handle: Handle, ptr, n: int, info: int, stats: dict):
+        self.gen = None
         self.handle = handle
         self._f = ptr
         self.n = n
@@ -346,6 +368,16 @@ class Factor:
         """B := A^{-1} B in FP64 (device B)."""
         _check(load().ooc_factor_solve(self.handle.ptr, self._f, _ptr(B), ldb, nrhs), "ooc_factor_solve")
 
+    def refine_gen(self, B, ldb: int, X, ldx: int, nrhs: int, tol: float = 1e-14, maxiter: int = 30):
+        """Refinement for a factor made by Handle.factor_gen: the residual regenerates A."""
+        seed, alpha = self.gen
+        it = ctypes.c_int(0)
+        be = ctypes.c_double(0)
+        _check(load().ooc_solve_refine_gen(self.handle.ptr, self._f, seed, alpha, _ptr(B), ldb, _ptr(X), ldx, nrhs,
+                                           float(tol), int(maxiter), ctypes.byref(it), ctypes.byref(be)),
+               "ooc_solve_refine_gen")
+        return it.value, be.value
+
     def refine(self, A, lda: int, B, ldb: int, X, ldx: int, nrhs: int, tol: float = 1e-14, maxiter: int = 30):
         """Iterative refinement to backward error <= tol; returns (iterations, backward error)."""
         it = ctypes.c_int(0)
@@ -354,3 +386,8 @@ class Factor:
                                        float(tol), int(maxiter), ctypes.byref(it), ctypes.byref(be)),
                "ooc_solve_refine")
         return it.value, be.value
+
+
+def factor_bytes(n: int, nb: int, prec="bf16x3") -> int:
+    p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+    return int(load().ooc_factor_bytes(n, nb, p))

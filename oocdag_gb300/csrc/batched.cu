@@ -31,10 +31,11 @@ constexpr int NMAX = 512;      // largest matrix order supported
 constexpr int NBUCKETS = 16;   // size buckets of 32: n in [32 q, 32 q + 31]
 
 struct Item {
-  i64 a_off;  // element offset of the matrix (column-major, ld = n)
-  i64 b_off;  // element offset of its right-hand side (overwritten by the solution)
+  void* a;    // the matrix (column-major, ld = n): A on entry, L on exit
+  void* b;    // its right-hand side (overwritten by the solution)
   int n;
   int blk;    // panel width for this matrix
+  int mode;   // 0: factor + solve, 1: solve with an L already in `a`
 };
 
 template <typename T>
@@ -188,8 +189,8 @@ __device__ void solve_one(const T* __restrict__ L, int n, T* __restrict__ b) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ items, int count, T* A, T* B,
-                                                     int* info, int* counter, int do_solve) {
+__global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ items, int count, int* info,
+                                                     int* counter, int do_solve) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   T* D = (T*)smem_raw;
   T* P = D + 64 * 65;
@@ -201,9 +202,10 @@ __global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ it
     __syncthreads();
     if (idx >= count) break;
     const Item it = items[idx];
-    const int f = factor_one<T>(A + it.a_off, it.n, it.blk, D, P, &s_fail);
+    T* a = (T*)it.a;
+    const int f = (it.mode == 0) ? factor_one<T>(a, it.n, it.blk, D, P, &s_fail) : 0;
     if (threadIdx.x == 0) info[idx] = f;
-    if (f == 0 && do_solve) solve_one<T>(A + it.a_off, it.n, B + it.b_off);
+    if (f == 0 && do_solve) solve_one<T>(a, it.n, (T*)it.b);
     __syncthreads();
   }
 }
@@ -218,20 +220,37 @@ template <typename T>
 size_t smem_for(int blk) { return (size_t)(64 * 65 + NMAX * (blk + 1)) * sizeof(T); }
 
 template <typename T>
+int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
+              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg);
+
+template <typename T>
 int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off, T* A, T* B,
                 int* info_host, const int* blk_table, int ctas_per_sm, int do_solve, double* seconds) {
-  cudaStream_t s = ooc_compute_stream(h);
+  std::vector<Item> items(count);
+  for (int i = 0; i < count; i++) items[i] = Item{(void*)(A + a_off[i]), (void*)(B + b_off[i]), n[i], 0, 0};
+  return run_items<T>(ooc_compute_stream(h), ooc_device(h), items, info_host, blk_table, ctas_per_sm, do_solve, seconds,
+                      [](void* hh, cudaStream_t st) { return ooc_wait_stream((ooc_handle*)hh, st); }, (void*)h);
+}
+
+// Sorts the items by decreasing order, picks each one's panel width from the table, and
+// runs them in one persistent launch on `s`; info_host receives LAPACK info per item in
+// the caller's order.
+template <typename T>
+int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
+              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg) {
+  const int count = (int)items_in.size();
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return items_in[x].n > items_in[y].n; });
   std::vector<Item> items(count);
   int maxblk = 1;
   for (int i = 0; i < count; i++) {
     const int j = order[i];
-    const int bucket = std::min(NBUCKETS - 1, n[j] / 32);
+    const int bucket = std::min(NBUCKETS - 1, items_in[j].n / 32);
     int blk = blk_table ? blk_table[bucket] : (sizeof(T) == 8 ? 32 : 64);
     blk = std::max(1, std::min(blk, sizeof(T) == 8 ? 32 : 64));
-    items[i] = Item{a_off[j], b_off[j], n[j], blk};
+    items[i] = items_in[j];
+    items[i].blk = blk;
     maxblk = std::max(maxblk, blk);
   }
   Item* d_items = nullptr;
@@ -253,7 +272,7 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
       cudaGetLastError();
       rc = OOC_ERR_UNSUPPORTED;
     } else {
-      int dev = ooc_device(h), nsm = 0;
+      int nsm = 0;
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       int occ = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_posv<T>, BT, sm);
@@ -262,7 +281,7 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
       cudaEventCreate(&e0);
       cudaEventCreate(&e1);
       cudaEventRecord(e0, s);
-      k_batched_posv<T><<<grid, BT, sm, s>>>(d_items, count, A, B, d_info, d_counter, do_solve);
+      k_batched_posv<T><<<grid, BT, sm, s>>>(d_items, count, d_info, d_counter, do_solve);
       cudaEventRecord(e1, s);
       k_scatter_info<<<(count + 255) / 256, 256, 0, s>>>(d_info, d_order, count, d_out);
       cudaError_t e = cudaGetLastError();
@@ -271,7 +290,7 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
   }
   if (!rc) {
     cudaMemcpyAsync(info_host, d_out, sizeof(int) * count, cudaMemcpyDeviceToHost, s);
-    rc = ooc_wait_stream(h, s);
+    rc = wait(wait_arg, s);
   }
   if (!rc && seconds) {
     float ms = 0;
@@ -301,6 +320,19 @@ int check_args(int count, const int* n, const int64_t* a_off, const int64_t* b_o
 }
 
 }  // namespace
+
+// Server hook: FP64 items given by absolute device pointers (mode 0 factor+solve, 1 solve).
+int ooc_batched_run_ptrs(cudaStream_t s, int dev, int count, double* const* a, double* const* b, const int* n,
+                         const int* mode, int* info_host, const int* blk_table) {
+  std::vector<Item> items(count);
+  for (int i = 0; i < count; i++) items[i] = Item{(void*)a[i], (void*)b[i], n[i], 0, mode[i]};
+  return run_items<double>(s, dev, items, info_host, blk_table, 0, 1, nullptr,
+                           [](void*, cudaStream_t st) -> int {
+                             cudaError_t e = cudaStreamSynchronize(st);
+                             return e == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+                           },
+                           nullptr);
+}
 
 extern "C" int ooc_batched_dposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,
                                  double* A, double* B, int* info, const int* blk_table, int ctas_per_sm,

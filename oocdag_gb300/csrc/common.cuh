@@ -96,3 +96,47 @@ int launch_gen_uniform_block(double* B, i64 ldb, i64 n, uint64_t seed, double al
                              i64 nc, cudaStream_t s);
 int launch_gen_pdmatgen_block(double* B, i64 ldb, i64 n, int seed, i64 r0, i64 c0, i64 m, i64 nc,
                               cudaStream_t s);
+
+// ---------------------------------------------------------------------------------
+// The uniform test matrix A = (R + R^T)/2 + alpha I element by element (the generator of
+// ooc_dmatgen_uniform), for kernels that regenerate A instead of storing it.
+// R(i,j) = u - 1/2, u = top 53 bits of SplitMix64 output number i + j*n, state started at
+// mix(seed); exact in binary64, so every user of these helpers sees the same bits.
+// ---------------------------------------------------------------------------------
+__host__ __device__ inline uint64_t ooc_sm64_mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__host__ __device__ inline uint64_t ooc_uniform_key(uint64_t seed) { return ooc_sm64_mix(seed + 0x9E3779B97F4A7C15ULL); }
+__device__ inline double ooc_r_elem(uint64_t key, uint64_t c) {
+  const uint64_t z = ooc_sm64_mix(key + (c + 1) * 0x9E3779B97F4A7C15ULL);
+  return __dadd_rn((double)(z >> 11) * 0x1.0p-53, -0.5);
+}
+__device__ inline double ooc_uniform_elem(uint64_t key, i64 n, double alpha, i64 i, i64 j) {
+  if (i == j) return __dadd_rn(ooc_r_elem(key, (uint64_t)(i + j * n)), alpha);
+  return __dmul_rn(0.5, __dadd_rn(ooc_r_elem(key, (uint64_t)(i + j * n)), ooc_r_elem(key, (uint64_t)(j + i * n))));
+}
+// b(i) ~ N(0,1) for right-hand sides: Box-Muller on two SplitMix64 uniforms of stream
+// `key`, element index i (column-major over the right-hand sides).
+__device__ inline double ooc_normal_elem(uint64_t key, uint64_t i) {
+  const uint64_t z1 = ooc_sm64_mix(key + (2 * i + 1) * 0x9E3779B97F4A7C15ULL);
+  const uint64_t z2 = ooc_sm64_mix(key + (2 * i + 2) * 0x9E3779B97F4A7C15ULL);
+  const double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;  // (0, 1)
+  const double u2 = (double)(z2 >> 11) * 0x1.0p-53;
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// Lower-triangular blocks (bi, bj), bj in [lo, hi), bi in [bj, T), enumerated column by
+// column: column c holds T - c blocks and S(c) = c T - c (c - 1) / 2 blocks precede it.
+__host__ __device__ inline i64 ooc_lower_blocks_before(i64 c, i64 T) { return c * T - c * (c - 1) / 2; }
+__device__ inline void ooc_lower_block_decode(i64 t, int T, int lo, int* bi, int* bj) {
+  const i64 u = t + ooc_lower_blocks_before(lo, T);
+  const double b = 2.0 * T + 1.0;
+  i64 c = (i64)floor((b - sqrt(fmax(b * b - 8.0 * (double)u, 0.0))) * 0.5);
+  if (c < 0) c = 0;
+  while (c > 0 && ooc_lower_blocks_before(c, T) > u) c--;
+  while (ooc_lower_blocks_before(c + 1, T) <= u) c++;
+  *bj = (int)c;
+  *bi = (int)(c + (u - ooc_lower_blocks_before(c, T)));
+}

@@ -19,31 +19,14 @@ namespace {
 // Uniform generator: R(i,j) = u - 1/2, u = top 53 bits of SplitMix64 output number
 // c = i + j*n (state started at mix(seed)); A = (R + R^T)/2 + alpha I.
 // ---------------------------------------------------------------------------------
-__host__ __device__ inline uint64_t sm64_mix(uint64_t z) {
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-  return z ^ (z >> 31);
-}
-__device__ inline double r_elem(uint64_t key, uint64_t c) {
-  uint64_t z = sm64_mix(key + (c + 1) * 0x9E3779B97F4A7C15ULL);
-  return __dadd_rn((double)(z >> 11) * 0x1.0p-53, -0.5);
-}
+__host__ __device__ inline uint64_t sm64_mix(uint64_t z) { return ooc_sm64_mix(z); }
 
 __global__ void k_gen_uniform(double* B, i64 ldb, i64 n, uint64_t key, double alpha, i64 r0, i64 c0,
                               i64 m, i64 nc) {
   const i64 ii = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (ii >= m) return;
   const i64 i = r0 + ii;
-  for (i64 jj = blockIdx.y; jj < nc; jj += gridDim.y) {
-    const i64 j = c0 + jj;
-    double v;
-    if (i == j) {
-      v = __dadd_rn(r_elem(key, (uint64_t)(i + j * n)), alpha);
-    } else {
-      v = __dmul_rn(0.5, __dadd_rn(r_elem(key, (uint64_t)(i + j * n)), r_elem(key, (uint64_t)(j + i * n))));
-    }
-    B[ii + jj * ldb] = v;
-  }
+  for (i64 jj = blockIdx.y; jj < nc; jj += gridDim.y) B[ii + jj * ldb] = ooc_uniform_elem(key, n, alpha, i, c0 + jj);
 }
 
 // ---------------------------------------------------------------------------------

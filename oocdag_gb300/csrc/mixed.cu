@@ -55,10 +55,10 @@ __device__ __forceinline__ void load_slab_f32(float* S, const float* X, i64 ldx,
 }
 
 __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, i64 ldx, double* __restrict__ C,
-                                                   i64 ldc, int m, int K, const int* status) {
+                                                   i64 ldc, int m, int K, int T, int bj_lo, const int* status) {
   if (status && *(volatile const int*)status) return;
   int bi, bj;
-  tri_decode(blockIdx.x, &bi, &bj);
+  ooc_lower_block_decode((i64)blockIdx.x, T, bj_lo, &bi, &bj);
   const int m0 = bi * FB, n0 = bj * FB;
   // 32 KB: double-buffered A and B slabs, reused afterwards to stage the result.
   __shared__ __align__(16) float smem[4 * FK * FB];
@@ -166,40 +166,55 @@ __global__ void k_to_f32(const double* __restrict__ X, i64 ldx, float* __restric
 constexpr int RMAX = 16;
 constexpr int NN_KCHUNK = 256;
 
-template <typename TA, typename TC>
+template <typename TA, typename TC, int R>
 __global__ void __launch_bounds__(256) k_gemm_nn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
                                                        i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
                                                        int kslice, TC* __restrict__ P, TC alpha, TC beta) {
-  __shared__ TC Bs[NN_KCHUNK * RMAX];
+  __shared__ TC Bs[NN_KCHUNK * R];
   const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   const int k0 = blockIdx.y * kslice;
   const int k1 = min(k, k0 + kslice);
-  TC acc[RMAX];
+  TC acc[R];
 #pragma unroll
-  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int q = 0; q < R; q++) acc[q] = 0;
+  const TA* Arow = A + (row < m ? row : 0);
   for (int kc = k0; kc < k1; kc += NN_KCHUNK) {
     const int kn = min(NN_KCHUNK, k1 - kc);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
       const int q = idx / kn, kk = idx % kn;
-      Bs[kk * RMAX + q] = B[(kc + kk) + (i64)q * ldb];
+      Bs[kk * R + q] = (q < r) ? B[(kc + kk) + (i64)q * ldb] : TC(0);
     }
     __syncthreads();
     if (row < m) {
-      for (int kk = 0; kk < kn; kk++) {
-        const TC a = (TC)A[row + (i64)(kc + kk) * lda];
+      int kk = 0;
+      // eight independent loads in flight per thread
+      for (; kk + 8 <= kn; kk += 8) {
+        TC a[8];
 #pragma unroll
-        for (int q = 0; q < RMAX; q++)
-          if (q < r) acc[q] = fma(a, Bs[kk * RMAX + q], acc[q]);
+        for (int u = 0; u < 8; u++) a[u] = (TC)Arow[(i64)(kc + kk + u) * lda];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[(kk + u) * R + q], acc[q]);
+      }
+      for (; kk < kn; kk++) {
+        const TC a = (TC)Arow[(i64)(kc + kk) * lda];
+#pragma unroll
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Bs[kk * R + q], acc[q]);
       }
     }
   }
   if (row >= m) return;
   if (P) {
     TC* Pz = P + (i64)blockIdx.y * m * r;
-    for (int q = 0; q < r; q++) Pz[row + (i64)q * m] = acc[q];
+#pragma unroll
+    for (int q = 0; q < R; q++)
+      if (q < r) Pz[row + (i64)q * m] = acc[q];
   } else {
-    for (int q = 0; q < r; q++) {
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      if (q >= r) break;
       TC* c = C + row + (i64)q * ldc;
       *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
     }
@@ -219,41 +234,53 @@ __global__ void k_reduce_slices(const TC* __restrict__ P, int nslice, TC* __rest
   }
 }
 
-template <typename TA, typename TC>
+template <typename TA, typename TC, int R>
 __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
                                                        i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
                                                        TC alpha, TC beta) {
-  __shared__ TC Bs[NN_KCHUNK * RMAX];
+  __shared__ TC Bs[NN_KCHUNK * R];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const i64 row = (i64)blockIdx.x * (blockDim.x / 32) + warp;
-  TC acc[RMAX];
+  TC acc[R];
 #pragma unroll
-  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int q = 0; q < R; q++) acc[q] = 0;
+  const TA* Acol = A + (row < m ? row : 0) * lda;
   for (int kc = 0; kc < k; kc += NN_KCHUNK) {
     const int kn = min(NN_KCHUNK, k - kc);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
       const int q = idx / kn, kk = idx % kn;
-      Bs[kk * RMAX + q] = B[(kc + kk) + (i64)q * ldb];
+      Bs[kk * R + q] = (q < r) ? B[(kc + kk) + (i64)q * ldb] : TC(0);
     }
     __syncthreads();
     if (row < m) {
-      for (int kk = lane; kk < kn; kk += 32) {
-        const TC a = (TC)A[(kc + kk) + row * lda];
+      int kk = lane;
+      for (; kk + 96 < kn; kk += 128) {
+        TC a[4];
 #pragma unroll
-        for (int q = 0; q < RMAX; q++)
-          if (q < r) acc[q] = fma(a, Bs[kk * RMAX + q], acc[q]);
+        for (int u = 0; u < 4; u++) a[u] = (TC)Acol[kc + kk + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[(kk + 32 * u) * R + q], acc[q]);
+      }
+      for (; kk < kn; kk += 32) {
+        const TC a = (TC)Acol[kc + kk];
+#pragma unroll
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Bs[kk * R + q], acc[q]);
       }
     }
   }
 #pragma unroll
-  for (int q = 0; q < RMAX; q++) {
+  for (int q = 0; q < R; q++) {
     TC v = acc[q];
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     acc[q] = v;
   }
   if (row >= m || lane != 0) return;
-  for (int q = 0; q < r; q++) {
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    if (q >= r) break;
     TC* c = C + row + (i64)q * ldc;
     *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
   }
@@ -323,6 +350,67 @@ __global__ void k_rowsum_abs(const double* A, i64 lda, int n, double* out) {
   out[i] = s;
 }
 
+// R(:, q) -= A(seed) X(:, q) over the columns [blockIdx.y * kslice, ...) of A, with A
+// regenerated element by element (uniform generator) instead of read from memory.
+// Partial sums per column slice go to P (nslice x m x r) for an ordered reduction.
+__global__ void __launch_bounds__(256) k_resid_gen(uint64_t key, i64 n, double alpha, const double* __restrict__ X,
+                                                   i64 ldx, int r, int kslice, double* __restrict__ P) {
+  __shared__ double Xs[NN_KCHUNK * RMAX];
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int k0 = blockIdx.y * kslice;
+  const int k1 = (int)min((i64)k0 + kslice, n);
+  double acc[RMAX];
+#pragma unroll
+  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int kc = k0; kc < k1; kc += NN_KCHUNK) {
+    const int kn = min(NN_KCHUNK, k1 - kc);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+      const int q = idx / kn, kk = idx % kn;
+      Xs[kk * RMAX + q] = X[(kc + kk) + (i64)q * ldx];
+    }
+    __syncthreads();
+    if (row < n) {
+      for (int kk = 0; kk < kn; kk++) {
+        const double a = ooc_uniform_elem(key, n, alpha, row, kc + kk);
+#pragma unroll
+        for (int q = 0; q < RMAX; q++)
+          if (q < r) acc[q] = fma(a, Xs[kk * RMAX + q], acc[q]);
+      }
+    }
+  }
+  if (row >= n) return;
+  double* Pz = P + (i64)blockIdx.y * n * r;
+  for (int q = 0; q < r; q++) Pz[row + (i64)q * n] = acc[q];
+}
+
+// Partial row sums of |A(seed)| over column slices (P: nslice x n).
+__global__ void __launch_bounds__(256) k_rowsum_gen(uint64_t key, i64 n, double alpha, int kslice,
+                                                    double* __restrict__ P) {
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const int k0 = blockIdx.y * kslice;
+  const int k1 = (int)min((i64)k0 + kslice, n);
+  double s = 0;
+  for (int c = k0; c < k1; c++) s += fabs(ooc_uniform_elem(key, n, alpha, row, c));
+  P[(i64)blockIdx.y * n + row] = s;
+}
+
+__global__ void k_sum_slices_rows(const double* __restrict__ P, int nslice, i64 n, double* __restrict__ out) {
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  double s = 0;
+  for (int z = 0; z < nslice; z++) s += P[(i64)z * n + row];
+  out[row] = s;
+}
+
+// B(i, q) = N(0,1) sample of stream `key`, element i + q*n.
+__global__ void k_gen_normal(double* B, i64 ldb, i64 n, int r, uint64_t key) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) B[i + q * ldb] = ooc_normal_elem(key, (uint64_t)(i + q * n));
+}
+
 }  // namespace
 
 // =================================================================================
@@ -330,7 +418,7 @@ __global__ void k_rowsum_abs(const double* A, i64 lda, int n, double* out) {
 // =================================================================================
 
 int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
-                       cudaStream_t s, void* work, size_t work_bytes);
+                       cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split);
 size_t bf16x3_work_bytes(int m, int K);
 
 namespace {
@@ -353,29 +441,54 @@ struct DevBuf {
   }
 };
 
+// C (lower, m x m) -= X X^T restricted to the 128-wide block columns [bj_lo, bj_hi) (bj_hi < 0
+// = all) in reduced precision.  `prepare` converts / splits X first; a second call on the
+// same X (another block-column range) may skip it.
 int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
-                 cudaStream_t s, DevBuf& work) {
+                 cudaStream_t s, DevBuf& work, int bj_lo = 0, int bj_hi = -1, int prepare = 1) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (prec == OOC_PREC_FP32) {
     const i64 ldy = ((i64)m + 3) / 4 * 4;
-    int rc = work.ensure((size_t)ldy * K * sizeof(float));
-    if (rc) return rc;
+    if (prepare) {
+      int rc = work.ensure((size_t)ldy * K * sizeof(float));
+      if (rc) return rc;
+    }
     float* Y = (float*)work.p;
-    k_to_f32<<<dim3((unsigned)((m + 255) / 256), (unsigned)std::min(K, 1024)), 256, 0, s>>>(X, ldx, Y, ldy, m, K);
+    if (prepare)
+      k_to_f32<<<dim3((unsigned)((m + 255) / 256), (unsigned)std::min(K, 1024)), 256, 0, s>>>(X, ldx, Y, ldy, m, K);
     const i64 T = ((i64)m + FB - 1) / FB;
-    const i64 nblk = T * (T + 1) / 2;
+    const i64 hi = std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
+    if (bj_lo >= hi) return OOC_OK;
+    const i64 nblk = ooc_lower_blocks_before(hi, T) - ooc_lower_blocks_before(bj_lo, T);
     if (nblk > 0x7fffffff) return OOC_ERR_INTERNAL;
-    k_syrk_f32<<<(unsigned)nblk, FTHR, 0, s>>>(Y, ldy, C, ldc, m, K, status);
+    k_syrk_f32<<<(unsigned)nblk, FTHR, 0, s>>>(Y, ldy, C, ldc, m, K, (int)T, bj_lo, status);
     OOC_CUDA_TRY(cudaGetLastError());
     return OOC_OK;
   }
   if (prec == OOC_PREC_BF16X3) {
-    int rc = work.ensure(bf16x3_work_bytes(m, K));
-    if (rc) return rc;
-    return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes);
+    if (prepare) {
+      int rc = work.ensure(bf16x3_work_bytes(m, K));
+      if (rc) return rc;
+    }
+    return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes, bj_lo, bj_hi, prepare);
   }
   return OOC_ERR_UNSUPPORTED;
 }
+
+// Instantiates a small-RHS kernel for the smallest of 1, 4, 16 columns covering r.
+#define NN_DISPATCH(r, launch)          \
+  do {                                  \
+    if ((r) <= 1) {                     \
+      constexpr int RR = 1;             \
+      launch;                           \
+    } else if ((r) <= 4) {              \
+      constexpr int RR = 4;             \
+      launch;                           \
+    } else {                            \
+      constexpr int RR = 16;            \
+      launch;                           \
+    }                                   \
+  } while (0)
 
 template <typename TA, typename TC>
 int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, int m, int k, int r, TC alpha, TC beta,
@@ -398,12 +511,12 @@ int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
     nslice = (k + kslice - 1) / kslice;
     int rc = part->ensure((size_t)nslice * m * r * sizeof(TC));
     if (rc) return rc;
-    k_gemm_nn_small<TA, TC><<<dim3(rows_blocks, nslice), 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, kslice,
-                                                                      (TC*)part->p, alpha, beta);
+    NN_DISPATCH(r, (k_gemm_nn_small<TA, TC, RR><<<dim3(rows_blocks, nslice), 256, 0, s>>>(
+                       A, lda, B, ldb, C, ldc, m, k, r, kslice, (TC*)part->p, alpha, beta)));
     k_reduce_slices<TC><<<rows_blocks, 256, 0, s>>>((const TC*)part->p, nslice, C, ldc, m, r, alpha, beta);
   } else {
-    k_gemm_nn_small<TA, TC><<<dim3(rows_blocks, 1), 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, k, nullptr,
-                                                                 alpha, beta);
+    NN_DISPATCH(r, (k_gemm_nn_small<TA, TC, RR><<<dim3(rows_blocks, 1), 256, 0, s>>>(
+                       A, lda, B, ldb, C, ldc, m, k, r, k, nullptr, alpha, beta)));
   }
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
@@ -414,7 +527,8 @@ int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
                   cudaStream_t s) {
   if (m <= 0 || r <= 0) return OOC_OK;
   if (r > RMAX) return OOC_ERR_UNSUPPORTED;
-  k_gemm_tn_small<TA, TC><<<(m + 7) / 8, 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, alpha, beta);
+  NN_DISPATCH(r, (k_gemm_tn_small<TA, TC, RR><<<(m + 7) / 8, 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, alpha,
+                                                                        beta)));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }
@@ -516,29 +630,34 @@ int alloc_factor(ooc_factor* F, i64 n, int nb, bool want_f32) {
   return OOC_OK;
 }
 
-// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and column solve and
-// trailing updates in `prec` (the reference's ooc_incore over the whole matrix,
-// oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-triangular update).
-// The column solve B := B L_jj^{-T} runs as one FP64 DMMA product with the tile's
-// inverse, B := W (L_jj^{-1})^T with W a copy of B, after the inverse (kept for the solves)
-// is formed from the diagonal tile alone; the triangular structure of L_jj^{-1} is
-// skipped in K, so the product costs the solve's own flops but runs as one parallel launch.
 struct MixedProf {
   bool on = false;
-  std::vector<cudaEvent_t> ev;  // pairs: [2k] start, [2k+1] end
+  std::vector<cudaEvent_t> ev;  // pairs: [2k] start, [2k+1] end (on the segment's stream)
   std::vector<int> kind;        // 0 = FP64 factor + column solve, 1 = trailing update
   std::vector<double> flops;    // algorithmic flops of each update
-  cudaEvent_t mark(cudaStream_t s) {
+  void mark(cudaStream_t s) {
     cudaEvent_t e;
     cudaEventCreate(&e);
     cudaEventRecord(e, s);
     ev.push_back(e);
-    return e;
   }
   ~MixedProf() { for (cudaEvent_t e : ev) cudaEventDestroy(e); }
 };
 
-int factor_mixed(ooc_factor* F, int prec, cudaStream_t s, int64_t* launches, MixedProf* prof) {
+// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and column solve and
+// trailing updates in `prec` (the reference's ooc_incore over the whole matrix,
+// oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-triangular update).
+//
+// The column solve B := B L_jj^{-T} runs as one FP64 DMMA product with the tile's inverse,
+// B := W (L_jj^{-1})^T with W a copy of B; the inverse (kept for the solves) is formed from
+// the diagonal tile alone, and the triangular structure of L_jj^{-1} is skipped in K.
+//
+// Look-ahead on two streams: the FP64 diagonal work of panel j (potrf, inverse, column
+// solve; FP64-pipe bound, few SMs for the small pieces) runs on `s1` while `s0` performs
+// the bulk of the trailing update of panel j-1 (HBM / tensor bound).  After each column
+// solve, `s0` first updates only the next panel's columns and signals `s1`, then updates
+// the rest.
+int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
   const int bb = (int)((n + nb - 1) / nb);
@@ -549,46 +668,78 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s, int64_t* launches, Mix
   if (rc) return rc;
   double* W = (double*)F->scratch.p;   // copy of the column panel (m x nb, ld n)
   double* E = W + (size_t)n * nb;      // L_jj^{-1} (lower, ld nb)
+  const bool split = (prec == OOC_PREC_FP64) || (nb % 128 == 0);
+  cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: panel solved (s1 -> s0)
+  OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
+  OOC_CUDA_TRY(cudaEventCreateWithFlags(&evP, cudaEventDisableTiming));
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+  } guard{evA, evP};
+  OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
   for (int j = 0; j < bb; j++) {
     const i64 J0 = (i64)j * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
     double* Djj = A + J0 + J0 * lda;
-    if (prof->on) { prof->mark(s); prof->kind.push_back(0); }
-    rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s);
+    // ---- s1: FP64 diagonal tile, its inverse, the column solve
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
+    if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
+    rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s1);
     if (rc) return rc;
-    // Dinv_j = I L_jj^{-T} = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
-    double* Dj = F->Dinv + (i64)j * tile;
-    k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s>>>(Dj, nb, LN);
-    rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s);
+    double* Dj = F->Dinv + (i64)j * tile;  // Dinv_j = I L_jj^{-T} = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
+    k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s1>>>(Dj, nb, LN);
+    rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s1);
     if (rc) return rc;
-    k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s>>>(Dj, nb, E, nb, LN);
+    k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s1>>>(Dj, nb, E, nb, LN);
     const i64 m = n - J0 - LN;
+    double* Pn = Djj + LN;  // the panel below the diagonal tile
     if (m > 0) {
-      double* Pn = Djj + LN;  // the panel below the diagonal tile
       OOC_CUDA_TRY(cudaMemcpy2DAsync(W, n * sizeof(double), Pn, lda * sizeof(double), m * sizeof(double), LN,
-                                     cudaMemcpyDeviceToDevice, s));
-      OOC_CUDA_TRY(cudaMemset2DAsync(Pn, lda * sizeof(double), 0, m * sizeof(double), LN, s));
-      rc = launch_gemm_nt_trib(W, n, E, nb, Pn, lda, (int)m, LN, LN, 1.0, F->status, s);
+                                     cudaMemcpyDeviceToDevice, s1));
+      OOC_CUDA_TRY(cudaMemset2DAsync(Pn, lda * sizeof(double), 0, m * sizeof(double), LN, s1));
+      rc = launch_gemm_nt_trib(W, n, E, nb, Pn, lda, (int)m, LN, LN, 1.0, F->status, s1);
       if (rc) return rc;
+    }
+    if (prof->on) prof->mark(s1);
+    OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+    // ---- s0: trailing update, next panel's columns first
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+    if (m > 0) {
+      double* C = A + (J0 + LN) * (1 + lda);
+      const int below = bb - j - 1;
       if (prof->on) {
-        prof->mark(s);
-        prof->mark(s);
+        prof->mark(s0);
         prof->kind.push_back(1);
         prof->flops.push_back((double)m * (double)(m + 1) * LN);
       }
       if (prec == OOC_PREC_FP64) {
-        TileMap C{A + (J0 + LN) * (1 + lda), lda, 0, bb - j - 1, nb};
-        rc = launch_panel_update(TileCol{Pn, lda, nb}, C, bb - j - 1, bb - j - 1, m, m, LN, F->status, s);
+        TileMap Cm{C, lda, 0, below, nb};
+        rc = launch_panel_update(TileCol{Pn, lda, nb}, Cm, below, 1, m, m, LN, F->status, s0);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+        if (below > 1) {
+          TileMap Cr{C + nb * (1 + lda), lda, 0, below - 1, nb};
+          rc = launch_panel_update(TileCol{Pn + nb, lda, nb}, Cr, below - 1, below - 1, m - nb, m - nb, LN,
+                                   F->status, s0);
+        }
+      } else if (split) {
+        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0);
       } else {
-        rc = syrk_lowprec(prec, Pn, lda, A + (J0 + LN) * (1 + lda), lda, (int)m, LN, F->status, s, F->work);
+        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
       }
       if (rc) return rc;
-      if (prof->on) prof->mark(s);
-    } else if (prof->on) {
-      prof->mark(s);
+      if (prof->on) prof->mark(s0);
     }
-    if (launches) *launches += 3 * ((LN + 63) / 64) + 2 * ((LN + 63) / 64) + 5;
+    if (launches) *launches += 5 * ((LN + 63) / 64) + 8;
   }
+  // s0 continues only after the last diagonal work on s1
+  OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+  OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
   return OOC_OK;
 }
 
@@ -600,12 +751,12 @@ int read_int(const int* d, int* h, cudaStream_t s) {
 
 }  // namespace
 
-extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int64_t lda, int nb, int prec,
-                                 ooc_factor** out, int* info, ooc_stats* stats) {
+static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, bool gen, uint64_t seed, double alpha,
+                       int nb, int prec, ooc_factor** out, int* info, ooc_stats* stats) {
   if (!h) return -1;
-  if (!A && n > 0) return -2;
+  if (!gen && !A && n > 0) return -2;
   if (n <= 0) return -3;
-  if (lda < n) return -4;
+  if (!gen && lda < n) return -4;
   if (nb <= 0) return -5;
   if (prec != OOC_PREC_FP64 && prec != OOC_PREC_FP32 && prec != OOC_PREC_BF16X3) return -6;
   if (!out) return -7;
@@ -627,10 +778,14 @@ extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int6
   cudaEventCreate(&e1);
   // copy A (host or device) into the factor's storage
   rc = OOC_OK;
-  if (cudaMemsetAsync(F->status, 0, sizeof(int), s) != cudaSuccess ||
-      cudaMemcpy2DAsync(F->L, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n, cudaMemcpyDefault,
-                        s) != cudaSuccess) {
-    rc = OOC_ERR_CUDA;
+  if (cudaMemsetAsync(F->status, 0, sizeof(int), s) != cudaSuccess) rc = OOC_ERR_CUDA;
+  if (!rc) {
+    if (gen) {
+      rc = launch_gen_uniform_block(F->L, n, n, seed, alpha, 0, 0, n, n, s);
+    } else if (cudaMemcpy2DAsync(F->L, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
+                                 cudaMemcpyDefault, s) != cudaSuccess) {
+      rc = OOC_ERR_CUDA;
+    }
   }
   int64_t launches = 0;
   MixedProf prof;
@@ -641,7 +796,9 @@ extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int6
   }
   if (!rc) {
     cudaEventRecord(e0, s);
-    rc = factor_mixed(F, prec, s, &launches, &prof);
+    void* s1p = nullptr;
+    ooc_get_stream(h, 1, &s1p);
+    rc = factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);
     if (!rc && F->Lf) {
       const int bb = (int)((n + nb - 1) / nb);
       k_copy_conv<double, float><<<dim3((unsigned)((n + 255) / 256), 1024), 256, 0, s>>>(F->L, n, F->Lf, n, (int)n,
@@ -682,6 +839,26 @@ extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int6
   }
   *out = F;
   return OOC_OK;
+}
+
+extern "C" int ooc_factor_create(ooc_handle* h, const double* A, int64_t n, int64_t lda, int nb, int prec,
+                                 ooc_factor** out, int* info, ooc_stats* stats) {
+  return create_impl(h, A, n, lda, false, 0, 0.0, nb, prec, out, info, stats);
+}
+
+extern "C" int ooc_factor_create_gen(ooc_handle* h, int64_t n, uint64_t seed, double alpha, int nb, int prec,
+                                     ooc_factor** out, int* info, ooc_stats* stats) {
+  return create_impl(h, nullptr, n, n, true, seed, alpha, nb, prec, out, info, stats);
+}
+
+extern "C" int64_t ooc_factor_bytes(int64_t n, int nb, int prec) {
+  if (n <= 0 || nb <= 0) return 0;
+  const int64_t bb = (n + nb - 1) / nb;
+  int64_t b = n * n * 8 + bb * nb * nb * 8 + (int64_t)nb * 16 * 8 + n * nb * 8 + (int64_t)nb * nb * 8;
+  if (prec != OOC_PREC_FP64) b += n * n * 4 + bb * nb * nb * 4 + (int64_t)nb * 16 * 4;
+  if (prec == OOC_PREC_BF16X3) b += 2 * ((n + 127) / 128 * 128) * ((nb + 63) / 64 * 64) * 2;
+  if (prec == OOC_PREC_FP32) b += ((n + 3) / 4 * 4) * nb * 4;
+  return b;
 }
 
 extern "C" int ooc_factor_destroy(ooc_factor* F) {
@@ -744,28 +921,16 @@ double host_max(const std::vector<double>& v, int r, int q, int nb) {
 }
 }  // namespace
 
-// Solve A X = B to a normwise backward error <= tol by iterative refinement with the
-// factor: X0 from the factor in FP64, then repeat R = B - A X (FP64, A the original
-// matrix on the device), D = A_F^{-1} R with the factor (FP32 copy for a reduced-
-// precision factor, FP64 otherwise), X += D.  B, X: device, n x nrhs.  Writes the
-// number of refinement steps and the final backward error (max over columns).
-extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda, const double* B,
-                                int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
-                                double* berr) {
-  if (!h) return -1;
-  if (!F) return -2;
-  if (!A) return -3;
-  if (lda < F->n) return -4;
-  if (!B) return -5;
-  if (ldb < F->n) return -6;
-  if (!X) return -7;
-  if (ldx < F->n) return -8;
-  if (nrhs <= 0 || nrhs > RMAX) return -9;
-  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+// Iterative refinement to a normwise backward error <= tol: X0 from the factor in FP64,
+// then repeat R = B - A X (FP64), D = A_F^{-1} R with the factor (FP32 copy for a
+// reduced-precision factor, FP64 otherwise), X += D.  A is either stored (Astore != null,
+// ld lda) or regenerated from the uniform generator (key, alpha) inside the residual.
+static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 lda, bool gen, uint64_t key,
+                       double alpha, const double* B, i64 ldb, double* X, i64 ldx, int r, double tol, int maxiter,
+                       int* iters, double* berr) {
   cudaSetDevice(F->device);
   cudaStream_t s = ooc_compute_stream(h);
   const i64 n = F->n;
-  const int r = nrhs;
   double *R = nullptr, *red = nullptr, *rows = nullptr;
   float* Rf = nullptr;
   const int nred = 152;
@@ -780,31 +945,38 @@ extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, i
     return OOC_ERR_NOMEM;
   }
   int rc = OOC_OK;
-  std::vector<double> hv((size_t)nred * r), hrow;
+  std::vector<double> hv((size_t)nred * r);
   const unsigned gb = (unsigned)((n + 255) / 256);
-  auto colmax = [&](const double* V, i64 ld, std::vector<double>& out) -> int {
-    k_colmax_abs<<<nred, 256, 0, s>>>(V, ld, (int)n, r, red);
-    OOC_CUDA_TRY(cudaMemcpyAsync(hv.data(), red, hv.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  // column slices of the generated products (enough CTAs to fill the GPU)
+  const int gslices = std::max(1, std::min((int)((n + 1023) / 1024), (int)((4 * 304 + gb - 1) / gb)));
+  const int gks = (int)((n + gslices - 1) / gslices);
+  auto colmax = [&](const double* V, i64 ld, int cols, std::vector<double>& out) -> int {
+    k_colmax_abs<<<nred, 256, 0, s>>>(V, ld, (int)n, cols, red);
+    OOC_CUDA_TRY(cudaMemcpyAsync(hv.data(), red, (size_t)nred * cols * sizeof(double), cudaMemcpyDeviceToHost, s));
     int e = ooc_wait_stream(h, s);
     if (e) return e;
-    out.assign(r, 0.0);
-    for (int q = 0; q < r; q++) out[q] = host_max(hv, r, q, nred);
+    out.assign(cols, 0.0);
+    for (int q = 0; q < cols; q++) out[q] = host_max(hv, cols, q, nred);
     return OOC_OK;
   };
   // ||A||_inf
   double normA = 0;
   {
-    k_rowsum_abs<<<gb, 256, 0, s>>>(A, lda, (int)n, rows);
-    std::vector<double> rs(1);
-    k_colmax_abs<<<nred, 256, 0, s>>>(rows, n, (int)n, 1, red);
-    std::vector<double> tmpv(nred);
-    OOC_CUDA_TRY(cudaMemcpyAsync(tmpv.data(), red, nred * sizeof(double), cudaMemcpyDeviceToHost, s));
-    rc = ooc_wait_stream(h, s);
-    for (double v : tmpv) normA = std::max(normA, v);
+    if (gen) {
+      rc = F->part.ensure((size_t)gslices * n * sizeof(double));
+      if (!rc) {
+        k_rowsum_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, gks, (double*)F->part.p);
+        k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
+      }
+    } else {
+      k_rowsum_abs<<<gb, 256, 0, s>>>(Astore, lda, (int)n, rows);
+    }
+    std::vector<double> nv;
+    if (!rc) rc = colmax(rows, n, 1, nv);
+    if (!rc) normA = nv[0];
   }
   std::vector<double> nb_(r), nx(r), nr(r);
-  if (!rc) rc = colmax(B, ldb, nb_);
-  // X0 = A_F^{-1} B in FP64
+  if (!rc) rc = colmax(B, ldb, r, nb_);
   if (!rc) {
     OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
                                    cudaMemcpyDeviceToDevice, s));
@@ -815,11 +987,20 @@ extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, i
   while (!rc) {
     // R = B - A X (FP64)
     k_residual_init<<<gb, 256, 0, s>>>(B, ldb, R, n, (int)n, r);
-    rc = gemm_nn_small<double, double>(A, lda, X, ldx, R, n, (int)n, (int)n, r, -1.0, 1.0, s, &F->part);
+    if (gen) {
+      rc = F->part.ensure((size_t)gslices * n * r * sizeof(double));
+      if (rc) break;
+      k_resid_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, X, ldx, r, gks, (double*)F->part.p);
+      k_reduce_slices<double><<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, R, n, (int)n, r, -1.0, 1.0);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) { ooc_set_last_error(e, "generated residual", __FILE__, __LINE__); rc = OOC_ERR_CUDA; break; }
+    } else {
+      rc = gemm_nn_small<double, double>(Astore, lda, X, ldx, R, n, (int)n, (int)n, r, -1.0, 1.0, s, &F->part);
+      if (rc) break;
+    }
+    rc = colmax(R, n, r, nr);
     if (rc) break;
-    rc = colmax(R, n, nr);
-    if (rc) break;
-    rc = colmax(X, ldx, nx);
+    rc = colmax(X, ldx, r, nx);
     if (rc) break;
     be = 0;
     for (int q = 0; q < r; q++) {
@@ -827,7 +1008,6 @@ extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, i
       be = std::max(be, den > 0 ? nr[q] / den : 0.0);
     }
     if (be <= tol || it >= maxiter) break;
-    // D = A_F^{-1} R
     if (F->Lf) {
       k_to_f32_cols<<<gb, 256, 0, s>>>(R, n, Rf, n, (int)n, r);
       rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
@@ -849,6 +1029,51 @@ extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, i
   if (iters) *iters = it;
   if (berr) *berr = be;
   return OOC_OK;
+}
+
+extern "C" int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda, const double* B,
+                                int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
+                                double* berr) {
+  if (!h) return -1;
+  if (!F) return -2;
+  if (!A) return -3;
+  if (lda < F->n) return -4;
+  if (!B) return -5;
+  if (ldb < F->n) return -6;
+  if (!X) return -7;
+  if (ldx < F->n) return -8;
+  if (nrhs <= 0 || nrhs > RMAX) return -9;
+  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+  return refine_impl(h, F, A, lda, false, 0, 0.0, B, ldb, X, ldx, nrhs, tol, maxiter, iters, berr);
+}
+
+extern "C" int ooc_solve_refine_gen(ooc_handle* h, ooc_factor* F, uint64_t seed, double alpha, const double* B,
+                                    int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter,
+                                    int* iters, double* berr) {
+  if (!h) return -1;
+  if (!F) return -2;
+  if (!B) return -5;
+  if (ldb < F->n) return -6;
+  if (!X) return -7;
+  if (ldx < F->n) return -8;
+  if (nrhs <= 0 || nrhs > RMAX) return -9;
+  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+  return refine_impl(h, F, nullptr, 0, true, ooc_uniform_key(seed), alpha, B, ldb, X, ldx, nrhs, tol, maxiter, iters,
+                     berr);
+}
+
+extern "C" int ooc_gen_normal(ooc_handle* h, double* B, int64_t n, int64_t ldb, int nrhs, uint64_t seed) {
+  if (!h) return -1;
+  if (!B && n > 0) return -2;
+  if (n < 0) return -3;
+  if (ldb < std::max<int64_t>(1, n)) return -4;
+  if (nrhs < 0) return -5;
+  if (n == 0 || nrhs == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  k_gen_normal<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(B, ldb, n, nrhs, ooc_uniform_key(seed));
+  OOC_CUDA_TRY(cudaGetLastError());
+  return ooc_wait_stream(h, s);
 }
 
 // C (lower, n x n, device) := C - A A^T with A (n x k, device), trailing-update kernels of

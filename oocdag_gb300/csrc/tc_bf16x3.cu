@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -123,7 +124,7 @@ __global__ void k_split_bf16(const double* __restrict__ X, i64 ldx, __nv_bfloat1
 
 __global__ void __launch_bounds__(128, 1)
     k_syrk_bf16x3(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
-                  double* __restrict__ C, i64 ldc, int m, int Kp, int* status) {
+                  double* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -136,11 +137,9 @@ __global__ void __launch_bounds__(128, 1)
   int* n_consumed = abort_flag + 2;  // stages whose load the MMA thread saw complete
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // lower-triangular block index
-  int bi = (int)((sqrt(8.0 * (double)blockIdx.x + 1.0) - 1.0) * 0.5);
-  while ((bi + 1) * (bi + 2) / 2 <= (int)blockIdx.x) bi++;
-  while (bi * (bi + 1) / 2 > (int)blockIdx.x) bi--;
-  const int bj = blockIdx.x - bi * (bi + 1) / 2;
+  // lower-triangular block (bi, bj) of the requested block-column range
+  int bi, bj;
+  ooc_lower_block_decode((i64)blockIdx.x, T, bj_lo, &bi, &bj);
   const int m0 = bi * TB, n0 = bj * TB;
   const int nk = Kp / TK;
 
@@ -297,7 +296,7 @@ size_t bf16x3_work_bytes(int m, int K) {
 }
 
 int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
-                       void* work, size_t work_bytes) {
+                       void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (!status) return OOC_ERR_INTERNAL;
   int rc = get_encode();
@@ -307,9 +306,11 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
   if (work_bytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
   __nv_bfloat16* hi = (__nv_bfloat16*)work;
   __nv_bfloat16* lo = hi + (size_t)Mp * Kp;
-  dim3 sg((unsigned)(Kp / 32), (unsigned)(Mp / 32));
-  k_split_bf16<<<sg, dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp, Kp);
-  OOC_CUDA_TRY(cudaGetLastError());
+  if (do_split) {
+    dim3 sg((unsigned)(Kp / 32), (unsigned)(Mp / 32));
+    k_split_bf16<<<sg, dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp, Kp);
+    OOC_CUDA_TRY(cudaGetLastError());
+  }
   CUtensorMap mh, ml;
   if (make_map(&mh, hi, Mp, Kp) || make_map(&ml, lo, Mp, Kp)) {
     ooc_set_last_message("cuTensorMapEncodeTiled failed for the BF16 split planes");
@@ -321,8 +322,11 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
     attr = true;
   }
   const i64 T = Mp / TB;
-  const i64 nblk = T * (T + 1) / 2;
-  k_syrk_bf16x3<<<(unsigned)nblk, 128, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, const_cast<int*>(status));
+  bj_hi = (int)std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
+  if (bj_lo >= bj_hi) return OOC_OK;
+  const i64 nblk = ooc_lower_blocks_before(bj_hi, T) - ooc_lower_blocks_before(bj_lo, T);
+  k_syrk_bf16x3<<<(unsigned)nblk, 128, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo,
+                                                        const_cast<int*>(status));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }
