@@ -65,6 +65,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-ref", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip the configs[3] batched and configs[4] serving runs")
     a = p.parse_args()
     if a.n is None:
         a.n = 65536 if a.form == "mixed" else 24576
@@ -604,6 +605,16 @@ def run_mixed(args):
                "sample": f"n={ns_} nb={nb}: FP64 factor (the reference's QUARK task graph restated in C++) + "
                          f"dpotrs, {tc:.1f}s on {os.cpu_count()} host threads"}
 
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_extra:
+        for name, fn in (("batched_configs3", lambda: bench_batched(h, args)),
+                         ("serving_configs4", lambda: bench_serving(args))):
+            try:
+                extra[name] = fn()
+            except Exception as e:  # report, do not lose the headline
+                extra[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+            torch.cuda.empty_cache()
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -618,6 +629,7 @@ def run_mixed(args):
             "fp64": fp64, "errors": errors,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
             "factor_seconds_avg": fac_s / args.steps,
+            **extra,
         }
         print(json.dumps(line), flush=True)
     h.close()
@@ -626,6 +638,194 @@ def run_mixed(args):
 
         dist.destroy_process_group()
     return 0
+
+
+# ----------------------------------------------------------------------------------
+# configs[3]: batched small systems in one persistent launch
+# ----------------------------------------------------------------------------------
+def bench_batched(h, args, count=20000, reps=3):
+    """20000 SPD systems, n ~ U{16..512}, A = M M^T/n + I (M ~ N(0,1)), one N(0,1) RHS each,
+    FP64 and FP32; tile widths from the autotuner; results compared per matrix with the
+    plain per-matrix FP64 path (the factor object + FP64 solve)."""
+    import numpy as np
+    import torch
+
+    from oocdag_gb300 import autotune
+
+    rng = np.random.default_rng(args.seed)
+    ns = [int(x) for x in rng.integers(16, 513, size=count)]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(args.seed)
+    a_off, b_off, ao, bo = [], [], 0, 0
+    for n in ns:
+        a_off.append(ao)
+        b_off.append(bo)
+        ao += n * n
+        bo += n
+    A64 = torch.empty(ao, dtype=torch.float64, device="cuda")
+    B64 = torch.empty(bo, dtype=torch.float64, device="cuda")
+    by_n = {}
+    for i, n in enumerate(ns):
+        by_n.setdefault(n, []).append(i)
+    for n, idx in by_n.items():  # one batched product per distinct order
+        M = torch.randn((len(idx), n, n), dtype=torch.float64, device="cuda", generator=g)
+        A = torch.bmm(M, M.transpose(1, 2)) / n + torch.eye(n, dtype=torch.float64, device="cuda")
+        b = torch.randn((len(idx), n), dtype=torch.float64, device="cuda", generator=g)
+        for k, i in enumerate(idx):
+            A64[a_off[i]:a_off[i] + n * n] = A[k].reshape(-1)  # symmetric: row-major == column-major
+            B64[b_off[i]:b_off[i] + n] = b[k]
+        del M, A, b
+    flops = sum(n ** 3 / 3.0 for n in ns)
+    out = {"count": count, "n_range": [16, 512], "flops_total": flops, "data_gb_fp64": ao * 8 / 1e9}
+    t0 = time.perf_counter()
+    tables = {}
+    for prec in ("fp64", "fp32"):
+        tables[prec] = autotune.tune(h, prec, flops_per_bucket=5e8, reps=1)["table"]
+    out["autotune_seconds"] = time.perf_counter() - t0
+    out["autotune_tables"] = tables
+    results = {}
+    for prec in ("fp64", "fp32"):
+        Ab = A64 if prec == "fp64" else A64.float()
+        Bb = B64 if prec == "fp64" else B64.float()
+        Aw, Bw = torch.empty_like(Ab), torch.empty_like(Bb)
+        times = []
+        for r in range(args.warmup + reps):
+            Aw.copy_(Ab)
+            Bw.copy_(Bb)
+            info, sec = h.batched_posv(prec, ns, a_off, b_off, Aw, Bw, blk_table=tables[prec])
+            if any(info):
+                raise RuntimeError(f"batched {prec}: info != 0")
+            if r >= args.warmup:
+                times.append(sec)
+        t = sum(times) / len(times)
+        results[prec] = {"seconds": t, "tflops": flops / t / 1e12, "matrices_per_s": count / t,
+                         "x": Bw.double().cpu().numpy()}
+        del Aw, Bw
+    # per-matrix comparison with the plain per-matrix FP64 path on a sample
+    samp = list(range(0, count, max(1, count // 64)))
+    md = {"fp64": 0.0, "fp32": 0.0}
+    Ah = A64.cpu().numpy()
+    Bh = B64.cpu().numpy()
+    for i in samp:
+        n = ns[i]
+        Ai = np.asfortranarray(Ah[a_off[i]:a_off[i] + n * n].reshape((n, n), order="F"))
+        with h.factor(Ai, n, n, 64, "fp64") as F:
+            bd = torch.from_numpy(Bh[b_off[i]:b_off[i] + n].copy()).cuda().reshape(1, n)
+            F.solve(bd, n, 1)
+            xr = bd.cpu().numpy().ravel()
+        for prec in ("fp64", "fp32"):
+            xb = results[prec]["x"][b_off[i]:b_off[i] + n]
+            md[prec] = max(md[prec], float(np.abs(xb - xr).max() / np.abs(xr).max()))
+    for prec in ("fp64", "fp32"):
+        results[prec].pop("x")
+        results[prec]["max_rel_diff_vs_fp64_path"] = md[prec]
+    out["fp64"] = results["fp64"]
+    out["fp32"] = results["fp32"]
+    out["compared_matrices"] = len(samp)
+    # CPU: per-matrix LAPACK loop on a bounded sample, threaded over matrices
+    try:
+        import concurrent.futures as cf
+
+        import scipy.linalg as sla
+
+        cs = list(range(0, count, max(1, count // 2000)))
+
+        def one(i):
+            n = ns[i]
+            Ai = Ah[a_off[i]:a_off[i] + n * n].reshape((n, n))
+            c = sla.cho_factor(Ai, lower=True, check_finite=False)
+            sla.cho_solve(c, Bh[b_off[i]:b_off[i] + n], check_finite=False)
+
+        c0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+            list(ex.map(one, cs))
+        tc = time.perf_counter() - c0
+        fl = sum(ns[i] ** 3 / 3.0 for i in cs)
+        out["cpu_baseline"] = {"value": fl / tc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                               "kind": "lapack-loop", "sample": f"{len(cs)} of the {count} matrices, "
+                               f"scipy cho_factor/cho_solve threaded over matrices, {tc:.2f}s"}
+    except Exception as e:  # the box may lack scipy threads; the GPU numbers stand
+        out["cpu_baseline"] = {"error": str(e)[:200]}
+    del A64, B64
+    torch.cuda.empty_cache()
+    return out
+
+
+# ----------------------------------------------------------------------------------
+# configs[4]: the served request stream
+# ----------------------------------------------------------------------------------
+def make_trace(rate, seconds, seed, big_frac=0.01, repeat_frac=0.3, nmin=64, nmax=32768, nbig=131072):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    t, out, keys = 0.0, [], []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        if keys and rng.random() < repeat_frac:
+            k, n, ms = keys[int(rng.integers(0, len(keys)))]
+            out.append(dict(t=t, kind=1, n=n, matrix_seed=ms, rhs_seed=int(rng.integers(1, 2 ** 62)), key=k))
+            continue
+        n = nbig if rng.random() < big_frac else int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        k = len(keys) + 1
+        ms = int(rng.integers(1, 2 ** 62))
+        keys.append((k, n, ms))
+        out.append(dict(t=t, kind=0, n=n, matrix_seed=ms, rhs_seed=int(rng.integers(1, 2 ** 62)), key=k))
+    return out
+
+
+def run_trace(trace, prec, drain_s, workers=4, nb=512):
+    import numpy as np
+
+    from oocdag_gb300.server import Server
+
+    with Server(workers=workers, nb=nb, prec=prec, batch_window_ms=1.0) as S:
+        ids, done = {}, {}
+        t_start = time.perf_counter()
+        i = 0
+        end = trace[-1]["t"] if trace else 0.0
+        while True:
+            now = time.perf_counter() - t_start
+            while i < len(trace) and trace[i]["t"] <= now:
+                q = trace[i]
+                ids[S.submit(q["n"], q["matrix_seed"], q["rhs_seed"], q["key"], q["kind"])] = q
+                i += 1
+            for c in S.poll(wait_ms=1):
+                done[c["id"]] = c
+            if i >= len(trace) and (len(done) == len(ids) or now > end + drain_s):
+                break
+        wall = time.perf_counter() - t_start
+        st = S.status()
+    ok = [c for c in done.values() if c["status"] == 0 and c["info"] == 0]
+    lat = np.array([c["t_done"] - c["t_submit"] for c in ok]) * 1e3
+    big = [c for c in ok if ids[c["id"]]["n"] > 32768]
+    res = {"prec": prec, "offered": len(trace), "completed": len(ok),
+           "refused": sum(1 for c in done.values() if c["status"] != 0),
+           "not_completed_in_run": len(trace) - len(done), "wall_s": wall,
+           "solves_per_s": len(ok) / wall if wall > 0 else None,
+           "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+           "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+           "max_backward_error": max((c["backward_error"] for c in ok), default=None),
+           "over_tolerance": sum(1 for c in ok if c["backward_error"] > 1e-14),
+           "batched_path": sum(1 for c in ok if c["path"] == 0),
+           "factor_reused": sum(1 for c in ok if c["factor_reused"]),
+           "big_completed": len(big), "server_state_at_end": st}
+    return res
+
+
+def bench_serving(args, seconds=10.0, drain_s=20.0):
+    """configs[4]: Poisson 200 req/s, n log-uniform [64, 32768] + 1% n=131072, 30% repeats;
+    mixed form beside the plain FP64 form; plus a sustainable-rate run of the same mix
+    without the n=131072 requests, where the latency percentiles are meaningful."""
+    out = {"rate_req_s": 200, "seconds_of_arrivals": seconds, "drain_s": drain_s}
+    trace = make_trace(200, seconds, args.seed)
+    out["mixed"] = run_trace(trace, "bf16x3", drain_s)
+    out["fp64"] = run_trace(make_trace(200, seconds / 5, args.seed), "fp64", drain_s / 2)
+    out["fp64"]["note"] = "plain FP64 form on the first fifth of the same trace (it saturates at once)"
+    light = make_trace(20, seconds, args.seed + 1, big_frac=0.0)
+    out["sustainable_mixed_20req_s"] = run_trace(light, "bf16x3", drain_s)
+    return out
 
 
 def main():

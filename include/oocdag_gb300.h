@@ -71,7 +71,11 @@ const char* ooc_last_error_string(void);
 int ooc_last_info(ooc_handle* h);
 /* The handle's CUDA streams (which: 0 = compute, 1 = host-to-device copies,
  * 2 = device-to-host copies), as a cudaStream_t, so that a caller can order its own
- * work or timing events against the library's.                                     */
+ * work or timing events against the library's.
+ * Device-pointer arguments are read on these streams (compute and host-to-device)
+ * from the moment of the call: data still being produced on another stream must be
+ * finished, or those two streams made to wait for it (cudaStreamWaitEvent), before
+ * the call.  Every call returns after its own work on the device is done.           */
 int ooc_get_stream(ooc_handle* h, int which, void** stream);
 
 /* Lower Cholesky A = L L^T in place, out of core.
@@ -104,8 +108,9 @@ void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, cons
 int ooc_panel_plan(int64_t n, int nb, int64_t memBlock, int nx, int* out, int cap);
 
 /* ---- mixed precision: factor once, solve with FP64 iterative refinement -------- */
-/* Precision of the trailing syrk/gemm updates (the diagonal-tile potrf and the column
- * solve always run in FP64).                                                        */
+/* Precision of the trailing syrk/gemm updates.  The diagonal-tile potrf and its inverse
+ * always run in FP64; the column solve (a product with that inverse) runs in FP64 for
+ * OOC_PREC_FP64 and in FP32 for the reduced-precision factors.                       */
 enum {
   OOC_PREC_FP64 = 0,  /* FP64 DMMA updates (the plain path)                        */
   OOC_PREC_FP32 = 1,  /* FP32 operands, FP32 FFMA accumulation                      */
@@ -217,6 +222,8 @@ int ooc_server_solution(ooc_server* s, int64_t id, double* x, int64_t n);
 int ooc_server_status(ooc_server* s, int64_t* pending, int64_t* running, int64_t* resident_bytes,
                       int64_t* reserved_bytes);
 double ooc_server_now(ooc_server* s);
+/* Description of the last failed request (empty if none).                            */
+const char* ooc_server_last_error(ooc_server* s);
 int ooc_server_destroy(ooc_server* s);
 
 /* Size of the device array that ooc_dpotrf_L_static uses as its panel buffer.      */

@@ -207,6 +207,24 @@ class Handle:
         except Exception:
             pass
 
+    def _after_torch(self, *xs) -> None:
+        """The library runs on the handle's own streams.  When an argument is a CUDA tensor,
+        torch work that produced it may still be in flight on torch's current stream: make
+        the handle's compute and host-to-device streams wait for it (an event, no host
+        synchronisation).  Every call returns after its own streams finished, so results are
+        ready for torch afterwards."""
+        for x in xs:
+            if getattr(x, "is_cuda", False):
+                import torch
+
+                ev = torch.cuda.Event()
+                ev.record(torch.cuda.current_stream(x.device))
+                if getattr(self, "_ext_streams", None) is None:
+                    self._ext_streams = [torch.cuda.ExternalStream(self.stream(w), device=x.device) for w in (0, 1)]
+                for st in self._ext_streams:
+                    st.wait_event(ev)
+                return
+
     def stream(self, which: int = 0) -> int:
         """cudaStream_t of the handle (0 compute, 1 host-to-device, 2 device-to-host)."""
         p = ctypes.c_void_p()
@@ -226,19 +244,23 @@ class Handle:
         in core).  Returns the LAPACK info and the call's statistics."""
         info = ctypes.c_int(0)
         st = OocStats()
+        self._after_torch(A)
         rc = load().ooc_dpotrf_L(self._h, _ptr(A), n, lda, nb, budget, ctypes.byref(info), ctypes.byref(st))
         _check(rc, "ooc_dpotrf_L")
         return Result(info.value, st.as_dict())
 
     def matgen_uniform(self, A, n: int, lda: int, seed: int, alpha: float) -> None:
+        self._after_torch(A)
         _check(load().ooc_dmatgen_uniform(self._h, _ptr(A), n, lda, seed, float(alpha)), "ooc_dmatgen_uniform")
 
     def matgen_pdmatgen(self, A, n: int, lda: int, seed: int = 100) -> None:
+        self._after_torch(A)
         _check(load().ooc_dmatgen_pdmatgen(self._h, _ptr(A), n, lda, seed), "ooc_dmatgen_pdmatgen")
 
     def residual(self, L, n: int, lda: int, kind: str, seed: int, alpha: float = 0.0) -> float:
         r = ctypes.c_double()
         k = 0 if kind == "uniform" else 1
+        self._after_torch(L)
         _check(load().ooc_dresidual(self._h, _ptr(L), n, lda, k, seed, float(alpha), ctypes.byref(r)),
                "ooc_dresidual")
         return r.value
@@ -250,6 +272,7 @@ class Handle:
         F = ctypes.c_void_p()
         info = ctypes.c_int(0)
         st = OocStats()
+        self._after_torch(A)
         _check(load().ooc_factor_create(self._h, _ptr(A), n, lda, nb, p, ctypes.byref(F), ctypes.byref(info),
                                         ctypes.byref(st)), "ooc_factor_create")
         return Factor(self, F, n, info.value, st.as_dict())
@@ -267,11 +290,13 @@ class Handle:
         return f
 
     def gen_normal(self, B, n: int, ldb: int, nrhs: int, seed: int) -> None:
+        self._after_torch(B)
         _check(load().ooc_gen_normal(self._h, _ptr(B), n, ldb, nrhs, seed), "ooc_gen_normal")
 
     def dsyrk_ln(self, prec, n: int, k: int, A, lda: int, C, ldc: int) -> None:
         """C := C - A A^T (lower) on the device with the given update precision."""
         p = PRECISIONS[prec] if isinstance(prec, str) else int(prec)
+        self._after_torch(A, C)
         _check(load().ooc_dsyrk_ln(self._h, p, n, k, _ptr(A), lda, _ptr(C), ldc), "ooc_dsyrk_ln")
 
     def batched_posv(self, prec: str, ns, a_off, b_off, A, B, blk_table=None, ctas_per_sm: int = 0):
@@ -288,6 +313,7 @@ class Handle:
         if blk_table is not None:
             tbl = (ctypes.c_int * 16)(*[int(x) for x in blk_table])
         sec = ctypes.c_double(0)
+        self._after_torch(A, B)
         fn = load().ooc_batched_dposv if prec == "fp64" else load().ooc_batched_sposv
         _check(fn(self._h, count, n_arr, ao, bo, _ptr(A), _ptr(B), info, tbl, ctas_per_sm, ctypes.byref(sec)),
                "ooc_batched_posv")
@@ -362,10 +388,12 @@ class Factor:
             pass
 
     def copy_L(self, L, ldl: int) -> None:
+        self.handle._after_torch(L)
         _check(load().ooc_factor_copy_L(self._f, _ptr(L), ldl), "ooc_factor_copy_L")
 
     def solve(self, B, ldb: int, nrhs: int) -> None:
         """B := A^{-1} B in FP64 (device B)."""
+        self.handle._after_torch(B)
         _check(load().ooc_factor_solve(self.handle.ptr, self._f, _ptr(B), ldb, nrhs), "ooc_factor_solve")
 
     def refine_gen(self, B, ldb: int, X, ldx: int, nrhs: int, tol: float = 1e-14, maxiter: int = 30):
@@ -373,6 +401,7 @@ class Factor:
         seed, alpha = self.gen
         it = ctypes.c_int(0)
         be = ctypes.c_double(0)
+        self.handle._after_torch(B, X)
         _check(load().ooc_solve_refine_gen(self.handle.ptr, self._f, seed, alpha, _ptr(B), ldb, _ptr(X), ldx, nrhs,
                                            float(tol), int(maxiter), ctypes.byref(it), ctypes.byref(be)),
                "ooc_solve_refine_gen")
@@ -382,6 +411,7 @@ class Factor:
         """Iterative refinement to backward error <= tol; returns (iterations, backward error)."""
         it = ctypes.c_int(0)
         be = ctypes.c_double(0)
+        self.handle._after_torch(A, B, X)
         _check(load().ooc_solve_refine(self.handle.ptr, self._f, _ptr(A), lda, _ptr(B), ldb, _ptr(X), ldx, nrhs,
                                        float(tol), int(maxiter), ctypes.byref(it), ctypes.byref(be)),
                "ooc_solve_refine")

@@ -76,7 +76,8 @@ def tune(handle, prec: str = "fp64", flops_per_bucket: float = 4e9, reps: int = 
                 B = B0.clone()
                 info, sec = handle.batched_posv(prec, ns, a_off, b_off, A, B, blk_table=[blk] * NBUCKETS)
                 if any(info):
-                    raise RuntimeError(f"tuning batch not SPD (bucket {q})")
+                    bad = [(ns[i], info[i]) for i in range(len(ns)) if info[i]][:5]
+                    raise RuntimeError(f"batched {prec} blk={blk} bucket {q}: info != 0 for (n, info) {bad}")
                 ts.append(sec)
             t = min(ts)
             timings[q][blk] = t

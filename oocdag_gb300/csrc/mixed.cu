@@ -1,8 +1,9 @@
 // Mixed-precision factorization and FP64 solves with iterative refinement.
 //
-// The factorization keeps the structure of the plain path (diagonal-tile potrf and the
-// column solve in FP64, oocquark.cpp:393-410 in the reference) but runs the trailing
-// syrk/gemm updates (oocquark.cpp:346,351) in reduced precision:
+// The factorization keeps the structure of the plain path (diagonal-tile potrf in FP64,
+// then the column solve, oocquark.cpp:393-410 in the reference; the column solve is a
+// product with the tile's FP64 inverse, in FP32 for a reduced-precision factor) but runs
+// the trailing syrk/gemm updates (oocquark.cpp:346,351) in reduced precision:
 //   OOC_PREC_FP32  : FP32 copies of the column panel, FP32 FFMA products accumulated in
 //                    FP32, subtracted from the FP64 trailing matrix;
 //   OOC_PREC_BF16X3: hi/lo BF16 splits of the column panel, three tensor-core products
@@ -31,14 +32,6 @@ constexpr int FB = 128, FK = 16, FTHR = 256;
 __device__ __forceinline__ void cp_async16f(void* smem, const void* gmem, int src_bytes) {
   unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
-}
-
-__device__ __forceinline__ void tri_decode(int t, int* bi, int* bj) {
-  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while ((i + 1) * (i + 2) / 2 <= t) i++;
-  while (i * (i + 1) / 2 > t) i--;
-  *bi = i;
-  *bj = t - i * (i + 1) / 2;
 }
 
 __device__ __forceinline__ void load_slab_f32(float* S, const float* X, i64 ldx, int r0, int m, int k0, int K) {
@@ -145,6 +138,102 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
       }
     }
     __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Column solve of a reduced-precision factor, in place:  P (m x LN, FP64, ld ldp) :=
+// P E^T with E = L_jj^{-1} (LN x LN, FP64, lower, exact zeros above the diagonal, ld
+// lde), products in FP32 (operands rounded to FP32 as they are staged).  This is the
+// dtrsm task (oocquark.cpp:130) as a product with the kept inverse.  One CTA per
+// 128-row block walks the 128-column blocks from the last to the first: output block cb
+// needs P's columns k < 128 (cb + 1) only, which no block written before it touches.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P, i64 ldp, const double* __restrict__ E,
+                                                       i64 lde, int m, int LN, const int* status) {
+  if (status && *(volatile const int*)status) return;
+  __shared__ __align__(16) float smem[4 * FK * FB];  // A, B slabs (x2), reused as output stage
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int r0 = blockIdx.x * FB;
+  constexpr int PER = FK * FB / FTHR;  // 8 staged elements per thread and operand
+  for (int cb = (LN - 1) / FB; cb >= 0; cb--) {
+    const int c0 = cb * FB;
+    const int kend = min(LN, c0 + FB);
+    const int nslab = (kend + FK - 1) / FK;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+    double ra[PER], rb[PER];
+    auto fetch = [&](int k0) {
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int idx = tid + u * FTHR;
+        const int kc = idx / FB, x = idx % FB;
+        const int gk = k0 + kc;
+        ra[u] = (r0 + x < m && gk < kend) ? P[(r0 + x) + (i64)gk * ldp] : 0.0;
+        rb[u] = (c0 + x < LN && gk < kend) ? E[(c0 + x) + (i64)gk * lde] : 0.0;  // (E^T)(gk, c) = E(c, gk)
+      }
+    };
+    fetch(0);
+    for (int s = 0; s < nslab; s++) {
+      float* as_w = smem + (s & 1) * FK * FB;  // A slab; the B slab follows 2 FK FB later
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int idx = tid + u * FTHR;
+        as_w[idx] = (float)ra[u];
+        as_w[2 * FK * FB + idx] = (float)rb[u];
+      }
+      __syncthreads();
+      if (s + 1 < nslab) fetch((s + 1) * FK);
+      const float* as = as_w;
+      const float* bs = as_w + 2 * FK * FB;
+#pragma unroll
+      for (int k = 0; k < FK; k++) {
+        const float4 a0 = *reinterpret_cast<const float4*>(as + k * FB + ty * 4);
+        const float4 a1 = *reinterpret_cast<const float4*>(as + k * FB + 64 + ty * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(bs + k * FB + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(bs + k * FB + 64 + tx * 4);
+        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+          for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+      }
+    }
+    __syncthreads();  // every read of P's columns < kend is done before any store below
+    // Store through shared memory 32 columns at a time (stride 129) so each warp writes
+    // whole column segments (coalesced).
+    float* stage = smem;
+#pragma unroll
+    for (int qtr = 0; qtr < 4; qtr++) {
+      const int half = qtr >> 1;
+      const int lo_tx = (qtr & 1) * 8;
+      if (tx >= lo_tx && tx < lo_tx + 8) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int rr = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+#pragma unroll
+          for (int j = 0; j < 4; j++) stage[((tx - lo_tx) * 4 + j) * 129 + rr] = acc[i][half * 4 + j];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int cc = warp * 4 + u;
+        const int c = c0 + half * 64 + (qtr & 1) * 32 + cc;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int rr = lane + 32 * q;
+          if (c < LN && r0 + rr < m) P[(r0 + rr) + (i64)c * ldp] = (double)stage[cc * 129 + rr];
+        }
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -418,7 +507,8 @@ __global__ void k_gen_normal(double* B, i64 ldb, i64 n, int r, uint64_t key) {
 // =================================================================================
 
 int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
-                       cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split);
+                       cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split,
+                       int reserve_sms);
 size_t bf16x3_work_bytes(int m, int K);
 
 namespace {
@@ -444,8 +534,10 @@ struct DevBuf {
 // C (lower, m x m) -= X X^T restricted to the 128-wide block columns [bj_lo, bj_hi) (bj_hi < 0
 // = all) in reduced precision.  `prepare` converts / splits X first; a second call on the
 // same X (another block-column range) may skip it.
+// reserve_sms: SMs the persistent tensor-core kernel leaves free for concurrent work on
+// another stream (the next panel's diagonal factor).
 int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
-                 cudaStream_t s, DevBuf& work, int bj_lo = 0, int bj_hi = -1, int prepare = 1) {
+                 cudaStream_t s, DevBuf& work, int bj_lo = 0, int bj_hi = -1, int prepare = 1, int reserve_sms = 0) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (prec == OOC_PREC_FP32) {
     const i64 ldy = ((i64)m + 3) / 4 * 4;
@@ -470,7 +562,8 @@ int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, 
       int rc = work.ensure(bf16x3_work_bytes(m, K));
       if (rc) return rc;
     }
-    return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes, bj_lo, bj_hi, prepare);
+    return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes, bj_lo, bj_hi, prepare,
+                              reserve_sms);
   }
   return OOC_ERR_UNSUPPORTED;
 }
@@ -644,19 +737,23 @@ struct MixedProf {
   ~MixedProf() { for (cudaEvent_t e : ev) cudaEventDestroy(e); }
 };
 
-// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and column solve and
-// trailing updates in `prec` (the reference's ooc_incore over the whole matrix,
-// oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-triangular update).
+// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and trailing updates
+// in `prec` (the reference's ooc_incore over the whole matrix, oocquark.cpp:389-419, with
+// the dsyrk/dgemm tasks as one lower-triangular update).
 //
-// The column solve B := B L_jj^{-T} runs as one FP64 DMMA product with the tile's inverse,
-// B := W (L_jj^{-1})^T with W a copy of B; the inverse (kept for the solves) is formed from
-// the diagonal tile alone, and the triangular structure of L_jj^{-1} is skipped in K.
+// The column solve B := B L_jj^{-T} runs as one product with the tile's inverse (kept for
+// the solves, formed in FP64 from the diagonal tile alone): for OOC_PREC_FP64 an FP64 DMMA
+// product B := W (L_jj^{-1})^T with W a copy of B, the triangular half of K skipped; for a
+// reduced-precision factor an FP32 product in place.
 //
-// Look-ahead on two streams: the FP64 diagonal work of panel j (potrf, inverse, column
-// solve; FP64-pipe bound, few SMs for the small pieces) runs on `s1` while `s0` performs
-// the bulk of the trailing update of panel j-1 (HBM / tensor bound).  After each column
-// solve, `s0` first updates only the next panel's columns and signals `s1`, then updates
-// the rest.
+// Look-ahead on two streams.  FP64: the diagonal work of panel j (potrf, inverse, column
+// solve) runs on `s1` while `s0` performs the bulk of the trailing update of panel j-1.
+// Reduced precision: only potrf and inverse run on `s1` (latency-bound, few SMs; the
+// persistent tensor-core update leaves kChainSMs SMs free for them), the column solve
+// runs on `s0` with every SM.  In both, `s0` first updates only the next panel's block
+// columns and signals `s1`, then updates the rest.
+constexpr int kChainSMs = 8;
+
 int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
@@ -677,6 +774,57 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
     ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
   } guard{evA, evP};
   OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
+  if (prec != OOC_PREC_FP64) {
+    for (int j = 0; j < bb; j++) {
+      const i64 J0 = (i64)j * nb;
+      const int LN = (int)std::min<i64>(nb, n - J0);
+      double* Djj = A + J0 + J0 * lda;
+      // ---- s1: FP64 diagonal tile and its inverse, beside the bulk update of panel j-1
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
+      if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
+      rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s1);
+      if (rc) return rc;
+      double* Dj = F->Dinv + (i64)j * tile;  // Dinv_j = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
+      k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s1>>>(Dj, nb, LN);
+      rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s1);
+      if (rc) return rc;
+      k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s1>>>(Dj, nb, E, nb, LN);
+      if (prof->on) prof->mark(s1);
+      OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+      // ---- s0: column solve (FP32, in place), then the trailing update
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+      const i64 m = n - J0 - LN;
+      if (m > 0) {
+        double* Pn = Djj + LN;
+        if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
+        k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, E, nb, (int)m, LN, F->status);
+        OOC_CUDA_TRY(cudaGetLastError());
+        if (prof->on) {
+          prof->mark(s0);
+          prof->mark(s0);
+          prof->kind.push_back(1);
+          prof->flops.push_back((double)m * (double)(m + 1) * LN);
+        }
+        double* C = A + (J0 + LN) * (1 + lda);
+        if (split) {
+          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1, 0);
+          if (rc) return rc;
+          OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
+        } else {
+          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
+          if (rc) return rc;
+          OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+        }
+        if (rc) return rc;
+        if (prof->on) prof->mark(s0);
+      }
+      if (launches) *launches += 4 * ((LN + 63) / 64) + 8;
+    }
+    OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+    return OOC_OK;
+  }
   for (int j = 0; j < bb; j++) {
     const i64 J0 = (i64)j * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
@@ -712,25 +860,14 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
         prof->kind.push_back(1);
         prof->flops.push_back((double)m * (double)(m + 1) * LN);
       }
-      if (prec == OOC_PREC_FP64) {
-        TileMap Cm{C, lda, 0, below, nb};
-        rc = launch_panel_update(TileCol{Pn, lda, nb}, Cm, below, 1, m, m, LN, F->status, s0);
-        if (rc) return rc;
-        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-        if (below > 1) {
-          TileMap Cr{C + nb * (1 + lda), lda, 0, below - 1, nb};
-          rc = launch_panel_update(TileCol{Pn + nb, lda, nb}, Cr, below - 1, below - 1, m - nb, m - nb, LN,
-                                   F->status, s0);
-        }
-      } else if (split) {
-        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1);
-        if (rc) return rc;
-        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0);
-      } else {
-        rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
-        if (rc) return rc;
-        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+      TileMap Cm{C, lda, 0, below, nb};
+      rc = launch_panel_update(TileCol{Pn, lda, nb}, Cm, below, 1, m, m, LN, F->status, s0);
+      if (rc) return rc;
+      OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+      if (below > 1) {
+        TileMap Cr{C + nb * (1 + lda), lda, 0, below - 1, nb};
+        rc = launch_panel_update(TileCol{Pn + nb, lda, nb}, Cr, below - 1, below - 1, m - nb, m - nb, LN,
+                                 F->status, s0);
       }
       if (rc) return rc;
       if (prof->on) prof->mark(s0);

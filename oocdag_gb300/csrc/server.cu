@@ -2,8 +2,9 @@
 //
 // Requests (factor a new SPD matrix and solve, or solve again with a resident factor)
 // arrive at any time.  A scheduler thread admits them in arrival order against a device
-// memory budget (evicting least-recently-used resident factors that nobody is using), and
-// routes them:
+// memory budget (evicting least-recently-used resident factors that nobody is using; a
+// request that does not fit yet keeps waiting while later ones that fit are admitted),
+// and routes them:
 //   * small systems (n <= small_max_n) to a batcher thread that gathers everything admitted
 //     within a short window and runs it as ONE persistent batched launch (factor+solve, or
 //     solve-only for resident factors), so requests that arrive while a batch runs join
@@ -25,6 +26,7 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -126,6 +128,7 @@ struct ooc_server {
   std::thread sched, batcher;
   std::vector<std::thread> workers;
   std::chrono::steady_clock::time_point t0;
+  std::string last_error;
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 
@@ -155,6 +158,12 @@ struct ooc_server {
 
   void complete(const Job& j, int status, int info, int path, int iters, double berr, double xsum,
                 std::vector<double>* x) {
+    if (status != OOC_OK) {
+      const char* m = ooc_last_error_string();
+      char buf[96];
+      snprintf(buf, sizeof(buf), "request %lld (n=%lld): status %d: ", (long long)j.id, (long long)j.r.n, status);
+      last_error = std::string(buf) + (m ? m : "");
+    }
     ooc_completion c{};
     c.id = j.id;
     c.status = status;
@@ -178,14 +187,12 @@ struct ooc_server {
     std::unique_lock<std::mutex> lk(mu);
     while (!stop) {
       cv_sched.wait_for(lk, std::chrono::milliseconds(1));
-      bool blocked_large = false;
       bool any_small = false, any_large = false;
       for (size_t i = 0; i < pending.size();) {
         Job& j = pending[i];
         j.small = j.r.n <= cfg.small_max_n;
         auto it = cache.find(j.r.key);
         const bool hit = j.r.kind == 1 && it != cache.end() && it->second.n == j.r.n && (it->second.F || it->second.Ls);
-        if (!j.small && blocked_large) { i++; continue; }
         const int64_t n = j.r.n;
         const int64_t need_f = hit ? 0 : (j.small ? 8 * n * n : ooc_factor_bytes(n, cfg.nb, cfg.prec));
         const int64_t need_w = j.small ? 64 * n : 64 * n + (64LL << 20);
@@ -197,7 +204,8 @@ struct ooc_server {
           continue;
         }
         if (!evict_for(need, hit ? j.r.key : -1)) {
-          if (!j.small) blocked_large = true;
+          // Does not fit now: it keeps its place; later requests that fit may pass it
+          // (a very large request waits until enough memory is free).
           i++;
           continue;
         }
@@ -341,7 +349,7 @@ struct ooc_server {
     double* Bbuf = nullptr;
     void* meta = nullptr;
     if (cudaMalloc(&Bbuf, std::max<int64_t>(btot, 1) * 8) != cudaSuccess ||
-        cudaMalloc(&meta, (size_t)count * (8 + 4 + 8 + 8 + 8 + 8)) != cudaSuccess) {
+        cudaMalloc(&meta, (size_t)count * (8 + 4 + 8 + 8 + 8 + 8) + 64) != cudaSuccess) {
       cudaGetLastError();
       status = OOC_ERR_NOMEM;
     }
@@ -360,6 +368,7 @@ struct ooc_server {
         }
         made[i] = true;
         status = launch_gen_uniform_block(Ls[i], n[i], n[i], batch[i].r.matrix_seed, (double)n[i], 0, 0, n[i], n[i], s);
+        if (status != OOC_OK) break;
       }
     }
     std::vector<double> berr(count, 0.0), xsum(count, 0.0);
@@ -377,18 +386,27 @@ struct ooc_server {
       double* d_be = (double*)mp;
       mp += (size_t)count * 8;
       double* d_xs = (double*)mp;
-      cudaMemcpyAsync(d_b, b.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(d_n, n.data(), (size_t)count * 4, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(d_ak, akey.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(d_bk, bkey.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s);
+      auto chk = [&](cudaError_t e, const char* what) {
+        if (e != cudaSuccess && status == OOC_OK) {
+          ooc_set_last_error(e, what, __FILE__, __LINE__);
+          status = OOC_ERR_CUDA;
+        }
+      };
+      chk(cudaMemcpyAsync(d_b, b.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s), "copy b pointers");
+      chk(cudaMemcpyAsync(d_n, n.data(), (size_t)count * 4, cudaMemcpyHostToDevice, s), "copy n");
+      chk(cudaMemcpyAsync(d_ak, akey.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s), "copy matrix keys");
+      chk(cudaMemcpyAsync(d_bk, bkey.data(), (size_t)count * 8, cudaMemcpyHostToDevice, s), "copy rhs keys");
       k_fill_normals<<<count, 128, 0, s>>>(d_b, d_n, d_bk, count);
-      status = ooc_batched_run_ptrs(s, cfg.device, count, Ls.data(), b.data(), n.data(), mode.data(), info.data(),
-                                    nullptr);
+      chk(cudaGetLastError(), "k_fill_normals");
+      if (status == OOC_OK)
+        status = ooc_batched_run_ptrs(s, cfg.device, count, Ls.data(), b.data(), n.data(), mode.data(), info.data(),
+                                      nullptr);
       if (status == OOC_OK) {
         k_small_berr<<<count, 256, 0, s>>>(d_b, d_n, d_ak, d_bk, count, d_be, d_xs);
-        cudaMemcpyAsync(berr.data(), d_be, (size_t)count * 8, cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(xsum.data(), d_xs, (size_t)count * 8, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) status = OOC_ERR_CUDA;
+        chk(cudaGetLastError(), "k_small_berr");
+        chk(cudaMemcpyAsync(berr.data(), d_be, (size_t)count * 8, cudaMemcpyDeviceToHost, s), "copy berr");
+        chk(cudaMemcpyAsync(xsum.data(), d_xs, (size_t)count * 8, cudaMemcpyDeviceToHost, s), "copy xsum");
+        chk(cudaStreamSynchronize(s), "batch synchronize");
       }
     }
     std::vector<std::vector<double>> xs(count);
@@ -515,6 +533,12 @@ extern "C" int ooc_server_status(ooc_server* S, int64_t* pending, int64_t* runni
 }
 
 extern "C" double ooc_server_now(ooc_server* S) { return S ? S->now() : 0.0; }
+
+extern "C" const char* ooc_server_last_error(ooc_server* S) {
+  if (!S) return "";
+  std::lock_guard<std::mutex> lk(S->mu);
+  return S->last_error.c_str();
+}
 
 extern "C" int ooc_server_destroy(ooc_server* S) {
   if (!S) return OOC_OK;

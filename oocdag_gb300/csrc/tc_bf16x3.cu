@@ -4,16 +4,23 @@
 //
 // X is split once per update into BF16 hi/lo planes (x = hi + lo + O(2^-17 |x|)), stored
 // K-major (each row's K values contiguous) so that TMA can stage 128 x 64 tiles with the
-// 128-byte swizzle the tensor core reads.  Each CTA owns one 128 x 128 block of the lower
-// triangle and accumulates, in TMEM (FP32),
+// 128-byte swizzle the tensor core reads.  For every 128 x 128 block of the lower
+// triangle the kernel accumulates, in TMEM (FP32),
 //     D = sum_k  Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T
-// with tcgen05.mma kind::f16 (M=128, N=128, K=16) issued by one thread, fed by a
-// two-stage TMA pipeline (mbarrier complete_tx), then reads D back with tcgen05.ld and
-// subtracts it from the FP64 block (one thread per row, coalesced along columns).
+// with tcgen05.mma kind::f16 (M=128, N=128, K=16) and subtracts D from the FP64 block.
+//
+// Persistent and warp-specialised: one CTA per SM walks the blocks in strips of 16 block
+// columns (row by row inside a strip, so the strip's B operands stay in L2 and each A
+// operand is reused by up to 16 consecutive blocks).  Warp 0 issues the TMA loads into a
+// three-stage ring, warp 1 (one elected thread) issues the MMAs into one of two TMEM
+// accumulators, and eight epilogue warps drain the other accumulator (tcgen05.ld) and do
+// the FP64 read-modify-write of C, so the HBM traffic of one block overlaps the MMAs of
+// the next.
 //
 // Every mbarrier wait is bounded.  A wait that runs out records an error code in the
-// status word (so every later kernel of the factorization returns at once), stops issuing
-// work, waits (bounded) for the MMAs already issued, frees its TMEM and returns.
+// status word (so every later kernel of the factorization returns at once), raises a
+// CTA-wide abort flag that ends every other role's loop, waits (bounded) for the MMAs and
+// TMA loads already issued, frees its TMEM and returns.
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -30,11 +37,15 @@ namespace {
 
 constexpr int TB = 128;        // output block (rows = cols)
 constexpr int TK = 64;         // K per stage: 64 bf16 = one 128-byte swizzle row
-constexpr int STAGES = 2;
+constexpr int STAGES = 3;
 constexpr int PLANE_BYTES = TB * TK * 2;          // 16 KB: one 128 x 64 bf16 tile
 constexpr int STAGE_BYTES = 4 * PLANE_BYTES;      // Ahi, Alo, Bhi, Blo
+constexpr int NACC = 2;                           // TMEM accumulators (double buffer)
+constexpr int TMEM_COLS = NACC * TB;
+constexpr int EPI_WARPS = 8;                      // two per TMEM lane quadrant
+constexpr int THREADS = 64 + 32 * EPI_WARPS;      // producer warp, MMA warp, epilogue
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr int TMEM_COLS = 128;
+constexpr int STRIP = 16;                         // block columns per scheduling strip
 constexpr long long WAIT_LIMIT = 1LL << 22;       // polls before a wait is declared stuck
 constexpr int ERR_TIMEOUT_CODE = -1000003;        // status value written on a stuck wait
 
@@ -48,8 +59,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
 }
-// Bounded parity wait: returns true when the phase with `parity` has completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded parity wait: true when the phase with `parity` has completed; false when the
+// poll limit runs out or another role raised the CTA's abort flag.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort_flag) {
   const uint32_t a = smem_u32(bar);
   for (long long i = 0; i < WAIT_LIMIT; i++) {
     uint32_t done;
@@ -59,8 +71,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
+    if (abort_flag && *abort_flag) return false;
   }
   return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
@@ -122,25 +139,54 @@ __global__ void k_split_bf16(const double* __restrict__ X, i64 ldx, __nv_bfloat1
   }
 }
 
-__global__ void __launch_bounds__(128, 1)
+// Block t of the lower-triangular block range [bj_lo, bj_hi) x rows (up to T), in strip
+// order: strips of STRIP block columns, and inside a strip row by row (the first rows of
+// a strip form its triangle).  Same set of blocks as ooc_lower_block_decode, other order.
+__device__ __forceinline__ void strip_block_decode(i64 t, int T, int bj_lo, int bj_hi, int* bi, int* bj) {
+  const int Tl = T - bj_lo, Wc = bj_hi - bj_lo;
+  for (int J0 = 0; J0 < Wc; J0 += STRIP) {
+    const i64 w = min(STRIP, Wc - J0);
+    const i64 tri = w * (w + 1) / 2;
+    const i64 cnt = tri + (i64)(Tl - J0 - w) * w;
+    if (t < cnt) {
+      int r, c;
+      if (t < tri) {
+        r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((i64)(r + 1) * (r + 2) / 2 <= t) r++;
+        while ((i64)r * (r + 1) / 2 > t) r--;
+        c = (int)(t - (i64)r * (r + 1) / 2);
+      } else {
+        const i64 u = t - tri;
+        r = (int)(w + u / w);
+        c = (int)(u % w);
+      }
+      *bi = bj_lo + J0 + r;
+      *bj = bj_lo + J0 + c;
+      return;
+    }
+    t -= cnt;
+  }
+  *bi = *bj = 0;  // not reached for t < number of blocks
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
     k_syrk_bf16x3(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
-                  double* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int* status) {
+                  double* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
+                  int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
-  uint64_t* empty = full + STAGES;
-  uint64_t* done = empty + STAGES;
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);  // TMA -> MMA, per stage
+  uint64_t* empty = full + STAGES;                            // MMA -> TMA, per stage
+  uint64_t* tfull = empty + STAGES;                           // MMA -> epilogue, per accumulator
+  uint64_t* tempty = tfull + NACC;                            // epilogue -> MMA, per accumulator
+  uint64_t* done = tempty + NACC;                             // drain after an abort
   uint32_t* tmem_slot = (uint32_t*)(done + 1);
-  int* abort_flag = (int*)(tmem_slot + 1);
-  int* n_issued = abort_flag + 1;    // stages loaded by the producer
-  int* n_consumed = abort_flag + 2;  // stages whose load the MMA thread saw complete
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  volatile long long* n_issued = (volatile long long*)(smem + STAGES * STAGE_BYTES + 128);  // stages loaded
+  volatile long long* n_consumed = n_issued + 1;  // stages whose load the MMA thread saw complete
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // lower-triangular block (bi, bj) of the requested block-column range
-  int bi, bj;
-  ooc_lower_block_decode((i64)blockIdx.x, T, bj_lo, &bi, &bj);
-  const int m0 = bi * TB, n0 = bj * TB;
   const int nk = Kp / TK;
 
   if (threadIdx.x == 0) {
@@ -148,13 +194,17 @@ __global__ void __launch_bounds__(128, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
+    for (int a = 0; a < NACC; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], EPI_WARPS);
+    }
     mbar_init(done, 1);
     *abort_flag = 0;
     *n_issued = 0;
     *n_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
@@ -164,99 +214,151 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {
-    // ---- TMA producer
-    for (int c = 0; c < nk; c++) {
-      const int s = c % STAGES;
-      const uint32_t ph = (uint32_t)((c / STAGES) & 1);
-      if (!mbar_wait(&empty[s], ph ^ 1)) { *(volatile int*)abort_flag = 1; break; }
-      if (*(volatile int*)abort_flag) break;
-      uint8_t* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_2d(st + 0 * PLANE_BYTES, &map_hi, &full[s], c * TK, m0);
-      tma_load_2d(st + 1 * PLANE_BYTES, &map_lo, &full[s], c * TK, m0);
-      tma_load_2d(st + 2 * PLANE_BYTES, &map_hi, &full[s], c * TK, n0);
-      tma_load_2d(st + 3 * PLANE_BYTES, &map_lo, &full[s], c * TK, n0);
-      *(volatile int*)n_issued = c + 1;
-    }
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer
-    int issued = 0;
-    for (int c = 0; c < nk; c++) {
-      const int s = c % STAGES;
-      const uint32_t ph = (uint32_t)((c / STAGES) & 1);
-      if (!mbar_wait(&full[s], ph)) { *(volatile int*)abort_flag = 1; break; }
-      *(volatile int*)n_consumed = c + 1;
-      if (*(volatile int*)abort_flag) break;
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-      const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t a_hi = base, a_lo = base + PLANE_BYTES, b_hi = base + 2 * PLANE_BYTES,
-                     b_lo = base + 3 * PLANE_BYTES;
-#pragma unroll
-      for (int kk = 0; kk < TK / 16; kk++) {
-        const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
-        const uint32_t acc0 = (c > 0 || kk > 0) ? 1u : 0u;
-        umma_bf16(tmem, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_hi + off), acc0);
-        umma_bf16(tmem, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_lo + off), 1u);
-        umma_bf16(tmem, umma_desc_sw128(a_lo + off), umma_desc_sw128(b_hi + off), 1u);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer
+      long long c = 0;
+      bool ok = true;
+      for (i64 t = blockIdx.x; ok && t < nblk; t += gridDim.x) {
+        int bi, bj;
+        strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+        const bool diag = (bi == bj);
+        for (int kc = 0; kc < nk; kc++, c++) {
+          const int s = (int)(c % STAGES);
+          const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) { ok = false; break; }
+          uint8_t* st = smem + s * STAGE_BYTES;
+          mbar_expect_tx(&full[s], diag ? 2 * PLANE_BYTES : STAGE_BYTES);
+          tma_load_2d(st + 0 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bi * TB);
+          tma_load_2d(st + 1 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bi * TB);
+          if (!diag) {  // a diagonal block's B operand is its A operand
+            tma_load_2d(st + 2 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bj * TB);
+            tma_load_2d(st + 3 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bj * TB);
+          }
+          *n_issued = c + 1;
+        }
       }
-      umma_commit(&empty[s]);  // stage free once these MMAs have read it
-      issued++;
+      if (!ok) *abort_flag = 1;
     }
-    umma_commit(done);  // fires when every MMA issued above has completed
-    (void)issued;
-  }
-  __syncwarp();
-
-  // ---- epilogue: all four warps
-  const bool ok = mbar_wait(done, 0);
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-  __syncthreads();
-  if (!ok || *(volatile int*)abort_flag) {
-    if (threadIdx.x == 0) {
-      atomicCAS(status, 0, ERR_TIMEOUT_CODE);
-      // Let loads still in flight land (bounded) before the CTA's shared memory goes away.
-      for (int c = *(volatile int*)n_consumed; c < *(volatile int*)n_issued; c++)
-        (void)mbar_wait(&full[c % STAGES], (uint32_t)((c / STAGES) & 1));
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      long long c = 0;
+      int tl = 0;
+      bool ok = true;
+      for (i64 t = blockIdx.x; ok && t < nblk; t += gridDim.x, tl++) {
+        int bi, bj;
+        strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+        const bool diag = (bi == bj);
+        const int acc = tl & 1;
+        if (!mbar_wait(&tempty[acc], (uint32_t)(((tl >> 1) & 1) ^ 1), abort_flag)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        const uint32_t dt = tmem + (uint32_t)(acc * TB);
+        for (int kc = 0; kc < nk; kc++, c++) {
+          const int s = (int)(c % STAGES);
+          const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
+          *n_consumed = c + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+          const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t a_hi = base, a_lo = base + PLANE_BYTES;
+          const uint32_t b_hi = diag ? a_hi : base + 2 * PLANE_BYTES;
+          const uint32_t b_lo = diag ? a_lo : base + 3 * PLANE_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; kk++) {
+            const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes along K inside the swizzle row
+            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+            umma_bf16(dt, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_hi + off), acc0);
+            umma_bf16(dt, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_lo + off), 1u);
+            umma_bf16(dt, umma_desc_sw128(a_lo + off), umma_desc_sw128(b_hi + off), 1u);
+          }
+          umma_commit(&empty[s]);  // stage free once these MMAs have read it
+        }
+        if (!ok) break;
+        umma_commit(&tfull[acc]);  // accumulator ready once every MMA above has completed
+      }
+      if (!ok) *abort_flag = 1;
     }
   } else {
-    const int row = m0 + warp * 32 + lane;
-    const bool diag = (bi == bj);
-#pragma unroll 1
-    for (int cb = 0; cb < TB; cb += 32) {
-      uint32_t v[32];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
-            "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-            "=r"(v[30]), "=r"(v[31])
-          : "r"(taddr));
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, half of the columns
+    const int quad = warp & 3;
+    const int chalf = ((warp - 2) >> 2) * (TB / 2);
+    int tl = 0;
+    for (i64 t = blockIdx.x; t < nblk; t += gridDim.x, tl++) {
+      int bi, bj;
+      strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+      const int acc = tl & 1;
+      const bool got = mbar_wait(&tfull[acc], (uint32_t)((tl >> 1) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+      uint32_t v[TB / 2];
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * TB + chalf);
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(v[32 * h + 0]), "=r"(v[32 * h + 1]), "=r"(v[32 * h + 2]), "=r"(v[32 * h + 3]),
+              "=r"(v[32 * h + 4]), "=r"(v[32 * h + 5]), "=r"(v[32 * h + 6]), "=r"(v[32 * h + 7]),
+              "=r"(v[32 * h + 8]), "=r"(v[32 * h + 9]), "=r"(v[32 * h + 10]), "=r"(v[32 * h + 11]),
+              "=r"(v[32 * h + 12]), "=r"(v[32 * h + 13]), "=r"(v[32 * h + 14]), "=r"(v[32 * h + 15]),
+              "=r"(v[32 * h + 16]), "=r"(v[32 * h + 17]), "=r"(v[32 * h + 18]), "=r"(v[32 * h + 19]),
+              "=r"(v[32 * h + 20]), "=r"(v[32 * h + 21]), "=r"(v[32 * h + 22]), "=r"(v[32 * h + 23]),
+              "=r"(v[32 * h + 24]), "=r"(v[32 * h + 25]), "=r"(v[32 * h + 26]), "=r"(v[32 * h + 27]),
+              "=r"(v[32 * h + 28]), "=r"(v[32 * h + 29]), "=r"(v[32 * h + 30]), "=r"(v[32 * h + 31])
+            : "r"(taddr + (uint32_t)(32 * h)));
+      }
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[acc]);  // the accumulator may be overwritten now
+      const int row = bi * TB + quad * 32 + lane;
+      const bool diag = (bi == bj);
       if (row < m) {
-        // All 32 loads first, then the stores: interleaved load/store pairs to possibly
-        // aliasing addresses would serialize on memory latency.
-        double* base = C + row + (i64)(n0 + cb) * ldc;
-        double cv[32];
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
-          const int col = n0 + cb + q;
-          cv[q] = (col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
-        }
+        for (int h = 0; h < 2; h++) {
+          // All 32 loads first, then the stores: interleaved load/store pairs to possibly
+          // aliasing addresses would serialize on memory latency.
+          const int c0 = bj * TB + chalf + 32 * h;
+          double* base = C + row + (i64)c0 * ldc;
+          double cv[32];
 #pragma unroll
-        for (int q = 0; q < 32; q++) {
-          const int col = n0 + cb + q;
-          if (col < m && (!diag || col <= row)) base[(i64)q * ldc] = cv[q] - (double)__uint_as_float(v[q]);
+          for (int q = 0; q < 32; q++) {
+            const int col = c0 + q;
+            cv[q] = (col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
+          }
+#pragma unroll
+          for (int q = 0; q < 32; q++) {
+            const int col = c0 + q;
+            if (col < m && (!diag || col <= row)) base[(i64)q * ldc] = cv[q] - (double)__uint_as_float(v[32 * h + q]);
+          }
         }
       }
+    }
+  }
+
+  // ---- teardown
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (*abort_flag) {
+    if (threadIdx.x == 0) atomicCAS(status, 0, ERR_TIMEOUT_CODE);
+    if (warp == 1 && lane == 0) {
+      umma_commit(done);  // fires once every MMA this thread issued has completed
+      (void)mbar_wait(done, 0, nullptr);
+    }
+    if (warp == 0 && lane == 0) {
+      // Let loads still in flight land (bounded) before the CTA's shared memory goes away.
+      for (long long c = *n_consumed; c < *n_issued; c++)
+        (void)mbar_wait(&full[c % STAGES], (uint32_t)((c / STAGES) & 1), nullptr);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
   __syncthreads();
-  if (warp == 0) {
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS));
   }
 }
@@ -296,7 +398,7 @@ size_t bf16x3_work_bytes(int m, int K) {
 }
 
 int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
-                       void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split) {
+                       void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split, int reserve_sms) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (!status) return OOC_ERR_INTERNAL;
   int rc = get_encode();
@@ -325,8 +427,12 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
   bj_hi = (int)std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
   if (bj_lo >= bj_hi) return OOC_OK;
   const i64 nblk = ooc_lower_blocks_before(bj_hi, T) - ooc_lower_blocks_before(bj_lo, T);
-  k_syrk_bf16x3<<<(unsigned)nblk, 128, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo,
-                                                        const_cast<int*>(status));
+  int dev = 0, nsm = 0;
+  OOC_CUDA_TRY(cudaGetDevice(&dev));
+  OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const i64 grid = std::max<i64>(1, std::min<i64>(nblk, std::max(1, nsm - std::max(0, reserve_sms))));
+  k_syrk_bf16x3<<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo, bj_hi, nblk,
+                                                            const_cast<int*>(status));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }

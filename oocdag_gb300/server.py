@@ -48,6 +48,8 @@ def _lib():
         L.ooc_server_now.argtypes = [P]
         L.ooc_server_now.restype = ctypes.c_double
         L.ooc_server_destroy.argtypes = [P]
+        L.ooc_server_last_error.argtypes = [P]
+        L.ooc_server_last_error.restype = ctypes.c_char_p
         _bound = True
     return L
 
@@ -97,6 +99,9 @@ class Server:
         v = [ctypes.c_int64() for _ in range(4)]
         _lib().ooc_server_status(self._s, *[ctypes.byref(x) for x in v])
         return dict(zip(["pending", "running", "resident_bytes", "reserved_bytes"], [x.value for x in v]))
+
+    def last_error(self) -> str:
+        return (_lib().ooc_server_last_error(self._s) or b"").decode()
 
     def now(self) -> float:
         return _lib().ooc_server_now(self._s)

@@ -93,3 +93,20 @@ def test_batched_block_table_does_not_change_results(handle):
         outs.append(Bd.cpu().numpy())
     for o in outs[1:]:
         assert np.abs(o - outs[0]).max() <= 1e-11 * np.abs(outs[0]).max()
+
+
+@pytest.mark.parametrize("blk", [8, 16, 32])
+def test_batched_every_width_all_buckets(handle, blk):
+    import torch
+
+    ns = list(range(16, 513, 7)) + [288, 289, 295, 300, 311, 319, 320]
+    mats, rhs, a_off, b_off, Af, Bf = _make_batch(ns, 17, np.float64)
+    Ad = torch.from_numpy(Af).cuda()
+    Bd = torch.from_numpy(Bf).cuda()
+    info, _ = handle.batched_posv("fp64", ns, a_off, b_off, Ad, Bd, blk_table=[blk] * 16)
+    bad = [(ns[i], info[i]) for i in range(len(ns)) if info[i]]
+    assert not bad, bad
+    Bh = Bd.cpu().numpy()
+    for i, n in enumerate(ns):
+        xref = np.linalg.solve(mats[i], rhs[i])
+        assert np.abs(Bh[b_off[i]:b_off[i] + n] - xref).max() <= 1e-11 * np.abs(xref).max(), (blk, n)
