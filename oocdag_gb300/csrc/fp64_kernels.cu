@@ -343,12 +343,8 @@ static int trsm_small_smem() { return (SB * SB + SB * 64) * (int)sizeof(double);
 static int launch_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB, int m, int m_last,
                              int batch, int n, const int* status, cudaStream_t s) {
   if (batch <= 0 || n <= 0) return OOC_OK;
-  static bool attr_set = false;  // per process; the attribute is per function
-  if (!attr_set) {
-    OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      trsm_small_smem()));
-    attr_set = true;
-  }
+  // per device: set on every launch (cheap)
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm_small, cudaFuncAttributeMaxDynamicSharedMemorySize, trsm_small_smem()));
   dim3 grid((max(m, m_last) + 63) / 64, batch);
   k_trsm_small<<<grid, 64, trsm_small_smem(), s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
   OOC_CUDA_TRY(cudaGetLastError());

@@ -237,6 +237,228 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Diagonal tile of a reduced-precision factor, fused in one CTA and in FP32:
+//   L_jj = chol(D) (the dpotrf task, oocquark.cpp:87/393), X = L_jj^{-1},
+// written back as FP64: D's lower triangle := L_jj, E := X (lower, zeros above, ld lde),
+// Dinv := X^T (upper, zeros below, ld lde).  FP64 runs at ~7 GFLOP/s per SM on this part,
+// FP32 at 64x that; the tile's rounding (~1e-7) is below the trailing updates' own.
+// Both phases are left-looking over 32-wide blocks, so every element is computed in
+// registers from finished data (L2-resident FP32 copies Lw, column-major, and Xr,
+// row-major, ld LN) and written once:
+//   phase 1, block column K: C = A(K:, K) - L(K:, :K) L(K, :K)^T (thread per row, the
+//            32 L(K, :K) rows staged in shared memory), one warp factors C's 32 x 32 top
+//            in registers, one thread per row solves the rows below;
+//   phase 2, block row I:    X(I, j) = -L_II^{-1} sum_q L(I, q) X(q, j) (thread per
+//            column j, the L(I, :I) rows staged), X(I, I) = L_II^{-1}.
+// A non-positive pivot writes info = col0 + j + 1 to the status word and stops.
+// ---------------------------------------------------------------------------------
+constexpr int DG_THREADS = 512, DG_B = 32, DG_LD = 33, DG_MAX = 512;
+constexpr size_t DG_SMEM = (size_t)(DG_MAX * DG_B + DG_MAX * DG_LD + 2 * DG_B * DG_LD + DG_B) * sizeof(float);
+
+// acc[c] -= sum_{q in [q_lo, q_hi)} v(q) * S[q * 32 + c], v(q) = src[q * stride] (L2), with
+// q_lo rounded down to 8 and v masked below q_lo; loads run one group of 8 ahead.
+__device__ __forceinline__ void dg_dot32(float acc[DG_B], const float* __restrict__ src, i64 stride, int q_lo,
+                                         int q_hi, const float* __restrict__ S, float sign) {
+  const int q0s = q_lo & ~7;
+  if (q0s >= q_hi) return;
+  float nx[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    const int q = q0s + u;
+    nx[u] = (q >= q_lo && q < q_hi) ? src[q * stride] : 0.f;
+  }
+  for (int q0 = q0s; q0 < q_hi; q0 += 8) {
+    float x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) x[u] = nx[u] * sign;
+    if (q0 + 8 < q_hi) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int q = q0 + 8 + u;
+        nx[u] = (q < q_hi) ? src[q * stride] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const float4* b4 = reinterpret_cast<const float4*>(S + (q0 + u) * DG_B);
+#pragma unroll
+      for (int v = 0; v < DG_B / 4; v++) {
+        const float4 bb = b4[v];
+        acc[4 * v + 0] = fmaf(x[u], bb.x, acc[4 * v + 0]);
+        acc[4 * v + 1] = fmaf(x[u], bb.y, acc[4 * v + 1]);
+        acc[4 * v + 2] = fmaf(x[u], bb.z, acc[4 * v + 2]);
+        acc[4 * v + 3] = fmaf(x[u], bb.w, acc[4 * v + 3]);
+      }
+    }
+  }
+}
+
+// S[q * 32 + c] = Lw(r0 + c, q) for q < nq, c < cb (0 for c >= cb): every load of the
+// thread is issued before the first store (a loop with one load per iteration would
+// wait an L2 round trip per element).
+__device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* __restrict__ Lw, i64 ldw, int r0,
+                                         int nq, int cb) {
+  constexpr int PER = DG_MAX * DG_B / DG_THREADS;  // 32 elements per thread at most
+  float v[PER];
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int idx = threadIdx.x + u * DG_THREADS;
+    const int q = idx >> 5, c = idx & 31;
+    v[u] = (q < nq && c < cb) ? Lw[(r0 + c) + q * ldw] : 0.f;
+  }
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int idx = threadIdx.x + u * DG_THREADS;
+    if ((idx >> 5) < nq) S[idx] = v[u];
+  }
+}
+
+__global__ void __launch_bounds__(DG_THREADS, 1)
+    k_diag_f32(double* __restrict__ D, i64 ldd, int LN, i64 col0, double* __restrict__ Dinv,
+               double* __restrict__ E, i64 lde, float* __restrict__ Lw, float* __restrict__ Xr, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(16) float dsm[];
+  float* S = dsm;                      // staged rows, q-major: S[q * 32 + r]
+  float* Cs = S + DG_MAX * DG_B;       // phase 1: the block column being finished, Cs[t * DG_LD + c]
+  float* Dk = Cs + DG_MAX * DG_LD;     // L(K, K), Dk[r * DG_LD + c]
+  float* Li = Dk + DG_B * DG_LD;       // phase 2: L_II^{-1}, Li[r * DG_LD + c]
+  float* dinv = Li + DG_B * DG_LD;     // 1 / L(k + c, k + c)
+  __shared__ int s_fail;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const i64 ldw = LN;
+  if (t == 0) s_fail = 0;
+  __syncthreads();
+  // ---- phase 1: L = chol(D), block columns left to right
+  for (int k0 = 0; k0 < LN; k0 += DG_B) {
+    const int kb = min(DG_B, LN - k0), mK = LN - k0;
+    dg_stage(S, Lw, ldw, k0, k0, kb);
+    __syncthreads();
+    if (t < mK) {
+      const int i = k0 + t;
+      float acc[DG_B];
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) acc[c] = (c < kb && c <= t) ? (float)D[i + (i64)(k0 + c) * ldd] : 0.f;
+      dg_dot32(acc, Lw + i, ldw, 0, k0, S, -1.f);
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) Cs[t * DG_LD + c] = acc[c];
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // 32 x 32 Cholesky in registers: lane r holds row r; column j travels by shuffles.
+      float a[DG_B];
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) a[c] = (lane < kb && c <= lane) ? Cs[lane * DG_LD + c] : 0.f;
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < DG_B; j++) {
+        if (j < kb && !bad) {
+          const float d = __shfl_sync(0xffffffffu, a[j], j);
+          if (!(d > 0.f)) {
+            bad = true;
+            if (lane == 0) { s_fail = 1; atomicCAS(status, 0, (int)(col0 + k0 + j + 1)); }
+          } else {
+            const float sq = sqrtf(d), inv = 1.f / sq;
+            if (lane == j) { a[j] = sq; dinv[j] = inv; }
+            if (lane > j) a[j] *= inv;
+#pragma unroll
+            for (int c = j + 1; c < DG_B; c++) {
+              const float lcj = __shfl_sync(0xffffffffu, a[j], c);
+              if (lane >= c) a[c] = fmaf(-a[j], lcj, a[c]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) Dk[lane * DG_LD + c] = (c <= lane) ? a[c] : 0.f;
+    }
+    __syncthreads();
+    if (s_fail) break;
+    if (t < mK) {
+      const int i = k0 + t;
+      float row[DG_B];
+      if (t < kb) {
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) row[c] = Dk[t * DG_LD + c];
+      } else {  // B := B L_KK^{-T}, one thread per row
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) row[c] = Cs[t * DG_LD + c];
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) {
+          float v = row[c];
+#pragma unroll
+          for (int q = 0; q < c; q++) v = fmaf(-row[q], Dk[c * DG_LD + q], v);
+          row[c] = v * dinv[c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < DG_B; c++)
+        if (c < kb && c <= t) {
+          Lw[i + (k0 + c) * ldw] = row[c];
+          D[i + (i64)(k0 + c) * ldd] = (double)row[c];
+        }
+    }
+    __syncthreads();
+  }
+  if (s_fail) return;
+  // ---- phase 2: X = L^{-1}, block rows top to bottom
+  for (int i0 = 0; i0 < LN; i0 += DG_B) {
+    const int ib = min(DG_B, LN - i0);
+    dg_stage(S, Lw, ldw, i0, i0, ib);
+    for (int idx = t; idx < DG_B * DG_B; idx += DG_THREADS) {
+      const int r = idx >> 5, c = idx & 31;
+      Dk[r * DG_LD + c] = (r < ib && c <= r) ? Lw[(i0 + r) + (i0 + c) * ldw] : 0.f;
+    }
+    __syncthreads();
+    if (warp == 0) {  // L_II^{-1}: lane c solves L_II x = e_c
+      float x[DG_B];
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) {
+        float v = (r == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int q = 0; q < r; q++) v = fmaf(-Dk[r * DG_LD + q], x[q], v);
+        x[r] = (r < ib) ? v / Dk[r * DG_LD + r] : 0.f;
+      }
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) Li[r * DG_LD + lane] = x[r];
+    }
+    __syncthreads();
+    if (t < i0) {
+      const int j = t;
+      float acc[DG_B];
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) acc[r] = 0.f;
+      dg_dot32(acc, Xr + j, ldw, j, i0, S, 1.f);  // acc[r] = sum_q L(i0 + r, q) X(q, j)
+      float y[DG_B];
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) {
+        float v = 0.f;
+#pragma unroll
+        for (int s2 = 0; s2 <= r; s2++) v = fmaf(Li[r * DG_LD + s2], acc[s2], v);
+        y[r] = -v;
+      }
+#pragma unroll
+      for (int r = 0; r < DG_B; r++)
+        if (r < ib) {
+          Xr[(i0 + r) * ldw + j] = y[r];
+          E[(i0 + r) + (i64)j * lde] = (double)y[r];
+          Dinv[j + (i64)(i0 + r) * lde] = (double)y[r];
+        }
+    } else if (t < LN) {
+      const int c = t - i0;  // diagonal block column (c < ib) or right of it (zeros)
+#pragma unroll
+      for (int r = 0; r < DG_B; r++)
+        if (r < ib) {
+          const float y = (c < ib && r >= c) ? Li[r * DG_LD + c] : 0.f;
+          if (c < ib) Xr[(i0 + r) * ldw + t] = y;
+          E[(i0 + r) + (i64)t * lde] = (double)y;
+          Dinv[t + (i64)(i0 + r) * lde] = (double)y;
+        }
+    }
+    __syncthreads();
+  }
+}
+
 // FP64 column panel (m x K, ld ldx) -> FP32 copy (ld ldy).
 __global__ void k_to_f32(const double* __restrict__ X, i64 ldx, float* __restrict__ Y, i64 ldy, int m, int K) {
   const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,14 +477,35 @@ __global__ void k_to_f32(const double* __restrict__ X, i64 ldx, float* __restric
 constexpr int RMAX = 16;
 constexpr int NN_KCHUNK = 256;
 
+// Optional copy done by the first CTA of a small product: dst(0:n, 0:r) := src (the
+// block a triangular-solve step has just finished, moved into place without a launch).
+template <typename TC>
+struct CopyOut {
+  const TC* src = nullptr;
+  i64 lds = 0;
+  TC* dst = nullptr;
+  i64 ldd = 0;
+  int n = 0;
+};
+
 template <typename TA, typename TC, int R>
 __global__ void __launch_bounds__(256) k_gemm_nn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
                                                        i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
-                                                       int kslice, TC* __restrict__ P, TC alpha, TC beta) {
-  __shared__ TC Bs[NN_KCHUNK * R];
-  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+                                                       int kslice, TC* __restrict__ P, TC alpha, TC beta,
+                                                       CopyOut<TC> co) {
+  // CTA: 32 rows x 8 warps; warp w sums its eighth of the CTA's k slice for the 32 rows
+  // (lane = row, so each load is 32 consecutive rows of one column); the eight partial
+  // sums are then added in warp order.
+  __shared__ TC Bs[NN_KCHUNK * R];  // also the 8 x 32 x R partial sums at the end
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const i64 row = (i64)blockIdx.x * 32 + lane;
   const int k0 = blockIdx.y * kslice;
   const int k1 = min(k, k0 + kslice);
+  if (co.n > 0 && blockIdx.x == 0 && blockIdx.y == 0)
+    for (int idx = threadIdx.x; idx < co.n * r; idx += blockDim.x) {
+      const int q = idx / co.n, i = idx % co.n;
+      co.dst[i + (i64)q * co.ldd] = co.src[i + (i64)q * co.lds];
+    }
   TC acc[R];
 #pragma unroll
   for (int q = 0; q < R; q++) acc[q] = 0;
@@ -275,10 +518,11 @@ __global__ void __launch_bounds__(256) k_gemm_nn_small(const TA* __restrict__ A,
       Bs[kk * R + q] = (q < r) ? B[(kc + kk) + (i64)q * ldb] : TC(0);
     }
     __syncthreads();
+    const int kw = (kn + 7) / 8;
+    const int ka = warp * kw, kb = min(kn, ka + kw);
     if (row < m) {
-      int kk = 0;
-      // eight independent loads in flight per thread
-      for (; kk + 8 <= kn; kk += 8) {
+      int kk = ka;
+      for (; kk + 8 <= kb; kk += 8) {
         TC a[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) a[u] = (TC)Arow[(i64)(kc + kk + u) * lda];
@@ -287,14 +531,26 @@ __global__ void __launch_bounds__(256) k_gemm_nn_small(const TA* __restrict__ A,
 #pragma unroll
           for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[(kk + u) * R + q], acc[q]);
       }
-      for (; kk < kn; kk++) {
+      for (; kk < kb; kk++) {
         const TC a = (TC)Arow[(i64)(kc + kk) * lda];
 #pragma unroll
         for (int q = 0; q < R; q++) acc[q] = fma(a, Bs[kk * R + q], acc[q]);
       }
     }
   }
-  if (row >= m) return;
+  static_assert(NN_KCHUNK == 8 * 32, "partial sums reuse the B chunk buffer");
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < R; q++) Bs[(warp * 32 + lane) * R + q] = acc[q];
+  __syncthreads();
+  if (warp != 0 || row >= m) return;
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    TC v = Bs[lane * R + q];
+#pragma unroll
+    for (int w = 1; w < 8; w++) v += Bs[(w * 32 + lane) * R + q];
+    acc[q] = v;
+  }
   if (P) {
     TC* Pz = P + (i64)blockIdx.y * m * r;
 #pragma unroll
@@ -326,9 +582,14 @@ __global__ void k_reduce_slices(const TC* __restrict__ P, int nslice, TC* __rest
 template <typename TA, typename TC, int R>
 __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A, i64 lda, const TC* __restrict__ B,
                                                        i64 ldb, TC* __restrict__ C, i64 ldc, int m, int k, int r,
-                                                       TC alpha, TC beta) {
+                                                       TC alpha, TC beta, CopyOut<TC> co) {
   __shared__ TC Bs[NN_KCHUNK * R];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (co.n > 0 && blockIdx.x == 0)
+    for (int idx = threadIdx.x; idx < co.n * r; idx += blockDim.x) {
+      const int q = idx / co.n, i = idx % co.n;
+      co.dst[i + (i64)q * co.ldd] = co.src[i + (i64)q * co.lds];
+    }
   const i64 row = (i64)blockIdx.x * (blockDim.x / 32) + warp;
   TC acc[R];
 #pragma unroll
@@ -585,7 +846,7 @@ int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, 
 
 template <typename TA, typename TC>
 int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, int m, int k, int r, TC alpha, TC beta,
-                  cudaStream_t s, DevBuf* part) {
+                  cudaStream_t s, DevBuf* part, CopyOut<TC> co = CopyOut<TC>()) {
   if (m <= 0 || r <= 0) return OOC_OK;
   if (r > RMAX) return OOC_ERR_UNSUPPORTED;
   if (k <= 0) {
@@ -594,22 +855,21 @@ int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
     }
     return OOC_OK;
   }
-  const int rows_blocks = (m + 255) / 256;
-  // Split the long k dimension when too few row blocks would fill the GPU.
-  int nslice = 1;
-  if (part && rows_blocks < 304 && k > 2 * NN_KCHUNK)
-    nslice = std::min((k + NN_KCHUNK - 1) / NN_KCHUNK, (304 + rows_blocks - 1) / rows_blocks);
+  const int rows_blocks = (m + 31) / 32;
+  // Long k: slices of at most 2048 (each warp then walks <= 256 columns) in grid.y, their
+  // partial sums added in slice order by k_reduce_slices.
+  int nslice = part ? (k + 2047) / 2048 : 1;
   if (nslice > 1) {
     const int kslice = ((k + nslice - 1) / nslice + NN_KCHUNK - 1) / NN_KCHUNK * NN_KCHUNK;
     nslice = (k + kslice - 1) / kslice;
     int rc = part->ensure((size_t)nslice * m * r * sizeof(TC));
     if (rc) return rc;
     NN_DISPATCH(r, (k_gemm_nn_small<TA, TC, RR><<<dim3(rows_blocks, nslice), 256, 0, s>>>(
-                       A, lda, B, ldb, C, ldc, m, k, r, kslice, (TC*)part->p, alpha, beta)));
-    k_reduce_slices<TC><<<rows_blocks, 256, 0, s>>>((const TC*)part->p, nslice, C, ldc, m, r, alpha, beta);
+                       A, lda, B, ldb, C, ldc, m, k, r, kslice, (TC*)part->p, alpha, beta, co)));
+    k_reduce_slices<TC><<<(m + 255) / 256, 256, 0, s>>>((const TC*)part->p, nslice, C, ldc, m, r, alpha, beta);
   } else {
     NN_DISPATCH(r, (k_gemm_nn_small<TA, TC, RR><<<dim3(rows_blocks, 1), 256, 0, s>>>(
-                       A, lda, B, ldb, C, ldc, m, k, r, k, nullptr, alpha, beta)));
+                       A, lda, B, ldb, C, ldc, m, k, r, k, nullptr, alpha, beta, co)));
   }
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
@@ -617,11 +877,11 @@ int gemm_nn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
 
 template <typename TA, typename TC>
 int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, int m, int k, int r, TC alpha, TC beta,
-                  cudaStream_t s) {
+                  cudaStream_t s, CopyOut<TC> co = CopyOut<TC>()) {
   if (m <= 0 || r <= 0) return OOC_OK;
   if (r > RMAX) return OOC_ERR_UNSUPPORTED;
   NN_DISPATCH(r, (k_gemm_tn_small<TA, TC, RR><<<(m + 7) / 8, 256, 0, s>>>(A, lda, B, ldb, C, ldc, m, k, r, alpha,
-                                                                        beta)));
+                                                                        beta, co)));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }
@@ -629,6 +889,10 @@ int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
 // Solve L L^T X = B in place (B: n x r, ld ldb) using the inverses of the diagonal
 // tiles.  Dinv_J holds L_JJ^{-T} (column-major, upper), i.e. the transpose of
 // L_JJ^{-1}; tmp holds nb x r.
+// B := (L L^T)^{-1} B with the factor's L and kept diagonal inverses (r <= 16 columns):
+// the dpotrs of the reference's VERIFY block (oocdag.cpp:439).  Two launches per block
+// step: the product with the block's inverse into tmp, then the panel product, whose
+// first CTA also moves tmp into place.
 template <typename T>
 int solve_with(const T* L, i64 ldl, const T* Dinv, i64 n, int nb, T* B, i64 ldb, int r, T* tmp, cudaStream_t s,
                DevBuf* part) {
@@ -639,31 +903,31 @@ int solve_with(const T* L, i64 ldl, const T* Dinv, i64 n, int nb, T* B, i64 ldb,
   for (int J = 0; J < bb; J++) {
     const i64 J0 = (i64)J * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
-    // y_J = L_JJ^{-1} b_J = Dinv_J^T b_J
-    rc = gemm_tn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s);
+    rc = gemm_tn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s);  // Dinv_J^T b_J
     if (rc) return rc;
-    OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
-                                   cudaMemcpyDeviceToDevice, s));
     const i64 rows = n - J0 - LN;
     if (rows > 0) {
-      rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, B + J0, ldb, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
-                               T(1), s, part);
+      rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, tmp, nb, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
+                               T(1), s, part, CopyOut<T>{tmp, nb, B + J0, ldb, LN});
       if (rc) return rc;
+    } else {
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+                                     cudaMemcpyDeviceToDevice, s));
     }
   }
   // backward: L^T x = y
   for (int J = bb - 1; J >= 0; J--) {
     const i64 J0 = (i64)J * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
-    // x_J = L_JJ^{-T} y_J = Dinv_J y_J
     rc = gemm_nn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s, nullptr);
     if (rc) return rc;
-    OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
-                                   cudaMemcpyDeviceToDevice, s));
-    if (J0 > 0) {
-      // y_{<J} -= L_{J,<J}^T x_J
-      rc = gemm_tn_small<T, T>(L + J0, ldl, B + J0, ldb, B, ldb, (int)J0, LN, r, T(-1), T(1), s);
+    if (J0 > 0) {  // y_{<J} -= L_{J,<J}^T x_J
+      rc = gemm_tn_small<T, T>(L + J0, ldl, tmp, nb, B, ldb, (int)J0, LN, r, T(-1), T(1), s,
+                               CopyOut<T>{tmp, nb, B + J0, ldb, LN});
       if (rc) return rc;
+    } else {
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+                                     cudaMemcpyDeviceToDevice, s));
     }
   }
   return OOC_OK;
@@ -766,6 +1030,8 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
   double* W = (double*)F->scratch.p;   // copy of the column panel (m x nb, ld n)
   double* E = W + (size_t)n * nb;      // L_jj^{-1} (lower, ld nb)
   const bool split = (prec == OOC_PREC_FP64) || (nb % 128 == 0);
+  if (prec != OOC_PREC_FP64)  // per device: set on every call (cheap)
+    OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
   cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: panel solved (s1 -> s0)
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evP, cudaEventDisableTiming));
@@ -782,13 +1048,21 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
       // ---- s1: FP64 diagonal tile and its inverse, beside the bulk update of panel j-1
       OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
       if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-      rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s1);
-      if (rc) return rc;
       double* Dj = F->Dinv + (i64)j * tile;  // Dinv_j = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
-      k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s1>>>(Dj, nb, LN);
-      rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s1);
-      if (rc) return rc;
-      k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s1>>>(Dj, nb, E, nb, LN);
+      if (LN <= DG_MAX) {
+        // FP32 potrf + inverse in one CTA; working copies in the (here unused) panel scratch
+        float* Lw = (float*)W;
+        k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, Dj, E, nb, Lw, Lw + (size_t)LN * LN,
+                                                   F->status);
+        OOC_CUDA_TRY(cudaGetLastError());
+      } else {
+        rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s1);
+        if (rc) return rc;
+        k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s1>>>(Dj, nb, LN);
+        rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s1);
+        if (rc) return rc;
+        k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s1>>>(Dj, nb, E, nb, LN);
+      }
       if (prof->on) prof->mark(s1);
       OOC_CUDA_TRY(cudaEventRecord(evP, s1));
       // ---- s0: column solve (FP32, in place), then the trailing update

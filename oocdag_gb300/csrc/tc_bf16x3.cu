@@ -13,7 +13,7 @@
 // columns (row by row inside a strip, so the strip's B operands stay in L2 and each A
 // operand is reused by up to 16 consecutive blocks).  Warp 0 issues the TMA loads into a
 // three-stage ring, warp 1 (one elected thread) issues the MMAs into one of two TMEM
-// accumulators, and eight epilogue warps drain the other accumulator (tcgen05.ld) and do
+// accumulators, and sixteen epilogue warps drain the other accumulator (tcgen05.ld) and do
 // the FP64 read-modify-write of C, so the HBM traffic of one block overlaps the MMAs of
 // the next.
 //
@@ -42,7 +42,7 @@ constexpr int PLANE_BYTES = TB * TK * 2;          // 16 KB: one 128 x 64 bf16 ti
 constexpr int STAGE_BYTES = 4 * PLANE_BYTES;      // Ahi, Alo, Bhi, Blo
 constexpr int NACC = 2;                           // TMEM accumulators (double buffer)
 constexpr int TMEM_COLS = NACC * TB;
-constexpr int EPI_WARPS = 8;                      // two per TMEM lane quadrant
+constexpr int EPI_WARPS = 16;                     // four per TMEM lane quadrant (32 columns each)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;      // producer warp, MMA warp, epilogue
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int STRIP = 16;                         // block columns per scheduling strip
@@ -215,31 +215,36 @@ __global__ void __launch_bounds__(THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    if (lane == 0) {
-      // ---- TMA producer
-      long long c = 0;
-      bool ok = true;
-      for (i64 t = blockIdx.x; ok && t < nblk; t += gridDim.x) {
-        int bi, bj;
-        strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
-        const bool diag = (bi == bj);
-        for (int kc = 0; kc < nk; kc++, c++) {
+    // ---- TMA producer (lane 0; the warp stays converged around it)
+    long long c = 0;
+    bool ok = true;
+    for (i64 t = blockIdx.x; ok && t < nblk; t += gridDim.x) {
+      int bi, bj;
+      strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+      const bool diag = (bi == bj);
+      for (int kc = 0; kc < nk; kc++, c++) {
+        if (lane == 0) {
           const int s = (int)(c % STAGES);
           const uint32_t ph = (uint32_t)((c / STAGES) & 1);
-          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) { ok = false; break; }
-          uint8_t* st = smem + s * STAGE_BYTES;
-          mbar_expect_tx(&full[s], diag ? 2 * PLANE_BYTES : STAGE_BYTES);
-          tma_load_2d(st + 0 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bi * TB);
-          tma_load_2d(st + 1 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bi * TB);
-          if (!diag) {  // a diagonal block's B operand is its A operand
-            tma_load_2d(st + 2 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bj * TB);
-            tma_load_2d(st + 3 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bj * TB);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+            ok = false;
+          } else {
+            uint8_t* st = smem + s * STAGE_BYTES;
+            mbar_expect_tx(&full[s], diag ? 2 * PLANE_BYTES : STAGE_BYTES);
+            tma_load_2d(st + 0 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bi * TB);
+            tma_load_2d(st + 1 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bi * TB);
+            if (!diag) {  // a diagonal block's B operand is its A operand
+              tma_load_2d(st + 2 * PLANE_BYTES, &map_hi, &full[s], kc * TK, bj * TB);
+              tma_load_2d(st + 3 * PLANE_BYTES, &map_lo, &full[s], kc * TK, bj * TB);
+            }
+            *n_issued = c + 1;
           }
-          *n_issued = c + 1;
         }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
       }
-      if (!ok) *abort_flag = 1;
     }
+    if (!ok && lane == 0) *abort_flag = 1;
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer
@@ -280,13 +285,27 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!ok) *abort_flag = 1;
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, half of the columns
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (block rows) and one quarter
+    // of the columns.  Each thread loads its 32 C values of the next block as soon as it
+    // has stored the current one, so the loads overlap that block's MMAs.
     const int quad = warp & 3;
-    const int chalf = ((warp - 2) >> 2) * (TB / 2);
+    const int cq = ((warp - 2) >> 2) * 32;
     int tl = 0;
-    for (i64 t = blockIdx.x; t < nblk; t += gridDim.x, tl++) {
-      int bi, bj;
-      strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+    i64 t = blockIdx.x;
+    int bi = 0, bj = 0;
+    double cv[32];
+    if (t < nblk) strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
+    {
+      const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
+      const bool diag = (bi == bj);
+      const double* base = C + row + (i64)c0 * ldc;
+#pragma unroll
+      for (int q = 0; q < 32; q++) {
+        const int col = c0 + q;
+        cv[q] = (t < nblk && row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
+      }
+    }
+    for (; t < nblk; t += gridDim.x, tl++) {
       const int acc = tl & 1;
       const bool got = mbar_wait(&tfull[acc], (uint32_t)((tl >> 1) & 1), abort_flag);
       if (!__all_sync(0xffffffffu, got)) {
@@ -294,47 +313,45 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-      uint32_t v[TB / 2];
-      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * TB + chalf);
+      // two halves of 16 columns: the first is stored before the second is read, which
+      // keeps the thread's registers within the 18-warp budget
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * TB + cq);
+      const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
+      const bool diag = (bi == bj);
+      double* base = C + row + (i64)c0 * ldc;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
+        uint32_t v[16];
         asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-            : "=r"(v[32 * h + 0]), "=r"(v[32 * h + 1]), "=r"(v[32 * h + 2]), "=r"(v[32 * h + 3]),
-              "=r"(v[32 * h + 4]), "=r"(v[32 * h + 5]), "=r"(v[32 * h + 6]), "=r"(v[32 * h + 7]),
-              "=r"(v[32 * h + 8]), "=r"(v[32 * h + 9]), "=r"(v[32 * h + 10]), "=r"(v[32 * h + 11]),
-              "=r"(v[32 * h + 12]), "=r"(v[32 * h + 13]), "=r"(v[32 * h + 14]), "=r"(v[32 * h + 15]),
-              "=r"(v[32 * h + 16]), "=r"(v[32 * h + 17]), "=r"(v[32 * h + 18]), "=r"(v[32 * h + 19]),
-              "=r"(v[32 * h + 20]), "=r"(v[32 * h + 21]), "=r"(v[32 * h + 22]), "=r"(v[32 * h + 23]),
-              "=r"(v[32 * h + 24]), "=r"(v[32 * h + 25]), "=r"(v[32 * h + 26]), "=r"(v[32 * h + 27]),
-              "=r"(v[32 * h + 28]), "=r"(v[32 * h + 29]), "=r"(v[32 * h + 30]), "=r"(v[32 * h + 31])
-            : "r"(taddr + (uint32_t)(32 * h)));
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr + (uint32_t)(16 * h)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+        if (h == 1) {
+          asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[acc]);  // the accumulator may be overwritten now
+        }
+        if (row < m) {
+#pragma unroll
+          for (int q = 0; q < 16; q++) {
+            const int col = c0 + 16 * h + q;
+            if (col < m && (!diag || col <= row))
+              base[(i64)(16 * h + q) * ldc] = cv[16 * h + q] - (double)__uint_as_float(v[q]);
+          }
+        }
       }
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty[acc]);  // the accumulator may be overwritten now
-      const int row = bi * TB + quad * 32 + lane;
-      const bool diag = (bi == bj);
-      if (row < m) {
+      const i64 tn = t + gridDim.x;
+      if (tn < nblk) {
+        strip_block_decode(tn, T, bj_lo, bj_hi, &bi, &bj);
+        const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
+        const bool diag = (bi == bj);
+        const double* base = C + row + (i64)c0 * ldc;
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          // All 32 loads first, then the stores: interleaved load/store pairs to possibly
-          // aliasing addresses would serialize on memory latency.
-          const int c0 = bj * TB + chalf + 32 * h;
-          double* base = C + row + (i64)c0 * ldc;
-          double cv[32];
-#pragma unroll
-          for (int q = 0; q < 32; q++) {
-            const int col = c0 + q;
-            cv[q] = (col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
-          }
-#pragma unroll
-          for (int q = 0; q < 32; q++) {
-            const int col = c0 + q;
-            if (col < m && (!diag || col <= row)) base[(i64)q * ldc] = cv[q] - (double)__uint_as_float(v[32 * h + q]);
-          }
+        for (int q = 0; q < 32; q++) {
+          const int col = c0 + q;
+          cv[q] = (row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
         }
       }
     }
@@ -418,11 +435,8 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
     ooc_set_last_message("cuTensorMapEncodeTiled failed for the BF16 split planes");
     return OOC_ERR_CUDA;
   }
-  static bool attr = false;
-  if (!attr) {
-    OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
+  // per device: set on every launch (cheap)
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   const i64 T = Mp / TB;
   bj_hi = (int)std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
   if (bj_lo >= bj_hi) return OOC_OK;
