@@ -113,9 +113,59 @@ __device__ inline double ooc_r_elem(uint64_t key, uint64_t c) {
   const uint64_t z = ooc_sm64_mix(key + (c + 1) * 0x9E3779B97F4A7C15ULL);
   return __dadd_rn((double)(z >> 11) * 0x1.0p-53, -0.5);
 }
+// Off-diagonal elements are integer multiples of 2^-54: A(i,j) = (r(i,j) + r(j,i)) / 2 with
+// r = u 2^-53 - 1/2 (u the top 53 bits of the SplitMix64 output) equals
+// (u(i,j) + u(j,i) - 2^53) 2^-54 exactly, since the sum of the two r's is exact in binary64.
+__device__ inline long long ooc_uniform_offdiag_int(uint64_t key, i64 n, i64 i, i64 j) {
+  const uint64_t u1 = ooc_sm64_mix(key + ((uint64_t)(i + j * n) + 1) * 0x9E3779B97F4A7C15ULL) >> 11;
+  const uint64_t u2 = ooc_sm64_mix(key + ((uint64_t)(j + i * n) + 1) * 0x9E3779B97F4A7C15ULL) >> 11;
+  return (long long)(u1 + u2) - (1LL << 53);
+}
+// ---- conversions on the integer pipe ------------------------------------------------
+// FP64 arithmetic and FP64 conversions share a pipe that runs at ~1/64 of FP32 on this
+// part, so the reduced-precision paths convert with integer operations (round to nearest
+// even, from the IEEE 754 encodings); the rare values outside the FP32 normal range take
+// the hardware conversion.
+__device__ __forceinline__ float ooc_f64_to_f32(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 126 || e > 1023 + 127) return __double2float_rn(x);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFULL;
+  unsigned int f = ((unsigned int)(b >> 63) << 31) | ((unsigned int)(e - 1023 + 127) << 23) | (unsigned int)(m >> 29);
+  const unsigned long long rem = m & 0x1FFFFFFFULL, half = 0x10000000ULL;
+  if (rem > half || (rem == half && (f & 1u))) f += 1u;  // a carry moves into the exponent (inf on overflow)
+  return __uint_as_float(f);
+}
+__device__ __forceinline__ double ooc_f32_to_f64(float x) {
+  const unsigned int f = __float_as_uint(x);
+  const unsigned int e = (f >> 23) & 0xFFu;
+  if ((f & 0x7FFFFFFFu) == 0) return __longlong_as_double((long long)((unsigned long long)(f >> 31) << 63));
+  if (e == 0 || e == 255) return (double)x;  // subnormal, inf, nan
+  const unsigned long long b = ((unsigned long long)(f >> 31) << 63) | ((unsigned long long)(e - 127 + 1023) << 52) |
+                               ((unsigned long long)(f & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
+// RN_f32(v 2^scale) for an integer |v| < 2^62 whose result is an FP32 normal number.
+__device__ __forceinline__ float ooc_i64_to_f32_scaled(long long v, int scale) {
+  if (v == 0) return 0.f;
+  const unsigned int sgn = v < 0 ? 1u : 0u;
+  unsigned long long a = sgn ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  a <<= lz;  // leading one at bit 63
+  unsigned int f = (sgn << 31) | ((unsigned int)(63 - lz + scale + 127) << 23) | ((unsigned int)(a >> 40) & 0x7FFFFFu);
+  const unsigned long long rem = a & 0xFFFFFFFFFFULL, half = 0x8000000000ULL;
+  if (rem > half || (rem == half && (f & 1u))) f += 1u;
+  return __uint_as_float(f);
+}
+
 __device__ inline double ooc_uniform_elem(uint64_t key, i64 n, double alpha, i64 i, i64 j) {
   if (i == j) return __dadd_rn(ooc_r_elem(key, (uint64_t)(i + j * n)), alpha);
-  return __dmul_rn(0.5, __dadd_rn(ooc_r_elem(key, (uint64_t)(i + j * n)), ooc_r_elem(key, (uint64_t)(j + i * n))));
+  return (double)ooc_uniform_offdiag_int(key, n, i, j) * 0x1.0p-54;
+}
+// RN_f32 of the same element (exact integer path off the diagonal).
+__device__ inline float ooc_uniform_elem_f32(uint64_t key, i64 n, double alpha, i64 i, i64 j) {
+  if (i == j) return ooc_f64_to_f32(__dadd_rn(ooc_r_elem(key, (uint64_t)(i + j * n)), alpha));
+  return ooc_i64_to_f32_scaled(ooc_uniform_offdiag_int(key, n, i, j), -54);
 }
 // b(i) ~ N(0,1) for right-hand sides: Box-Muller on two SplitMix64 uniforms of stream
 // `key`, element index i (column-major over the right-hand sides).

@@ -47,7 +47,8 @@ __device__ __forceinline__ void load_slab_f32(float* S, const float* X, i64 ldx,
   }
 }
 
-__global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, i64 ldx, double* __restrict__ C,
+template <typename TC>
+__global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, i64 ldx, TC* __restrict__ C,
                                                    i64 ldc, int m, int K, int T, int bj_lo, const int* status) {
   if (status && *(volatile const int*)status) return;
   int bi, bj;
@@ -123,18 +124,18 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
     for (int u = 0; u < 4; u++) {
       const int cc = warp * 4 + u;
       const int c = n0 + half * 64 + (qtr & 1) * 32 + cc;
-      double cv[4];
+      TC cv[4];
       bool ok[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int r = m0 + lane + 32 * q;
         ok[q] = (c < m) && (r < m) && !(bi == bj && c > r);
-        cv[q] = ok[q] ? C[r + (i64)c * ldc] : 0.0;
+        cv[q] = ok[q] ? C[r + (i64)c * ldc] : TC(0);
       }
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int rr = lane + 32 * q;
-        if (ok[q]) C[m0 + rr + (i64)c * ldc] = cv[q] - (double)stage[cc * 129 + rr];
+        if (ok[q]) C[m0 + rr + (i64)c * ldc] = cv[q] - (TC)stage[cc * 129 + rr];
       }
     }
     __syncthreads();
@@ -142,15 +143,14 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
 }
 
 // ---------------------------------------------------------------------------------
-// Column solve of a reduced-precision factor, in place:  P (m x LN, FP64, ld ldp) :=
-// P E^T with E = L_jj^{-1} (LN x LN, FP64, lower, exact zeros above the diagonal, ld
-// lde), products in FP32 (operands rounded to FP32 as they are staged).  This is the
-// dtrsm task (oocquark.cpp:130) as a product with the kept inverse.  One CTA per
+// Column solve of a reduced-precision factor, in place:  P (m x LN, FP32, ld ldp) :=
+// P E^T with E = L_jj^{-1} (LN x LN, FP32, lower, exact zeros above the diagonal, ld
+// lde).  This is the dtrsm task (oocquark.cpp:130) as a product with the kept inverse.  One CTA per
 // 128-row block walks the 128-column blocks from the last to the first: output block cb
 // needs P's columns k < 128 (cb + 1) only, which no block written before it touches.
 // ---------------------------------------------------------------------------------
-__global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P, i64 ldp, const double* __restrict__ E,
-                                                       i64 lde, int m, int LN, const int* status) {
+__global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P, i64 ldp, const float* __restrict__ E,
+                                                          i64 lde, int m, int LN, const int* status) {
   if (status && *(volatile const int*)status) return;
   __shared__ __align__(16) float smem[4 * FK * FB];  // A, B slabs (x2), reused as output stage
   const int tid = threadIdx.x;
@@ -167,15 +167,15 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P
     for (int i = 0; i < 8; i++)
 #pragma unroll
       for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
-    double ra[PER], rb[PER];
+    float ra[PER], rb[PER];
     auto fetch = [&](int k0) {
 #pragma unroll
       for (int u = 0; u < PER; u++) {
         const int idx = tid + u * FTHR;
         const int kc = idx / FB, x = idx % FB;
         const int gk = k0 + kc;
-        ra[u] = (r0 + x < m && gk < kend) ? P[(r0 + x) + (i64)gk * ldp] : 0.0;
-        rb[u] = (c0 + x < LN && gk < kend) ? E[(c0 + x) + (i64)gk * lde] : 0.0;  // (E^T)(gk, c) = E(c, gk)
+        ra[u] = (r0 + x < m && gk < kend) ? P[(r0 + x) + (i64)gk * ldp] : 0.f;
+        rb[u] = (c0 + x < LN && gk < kend) ? E[(c0 + x) + (i64)gk * lde] : 0.f;  // (E^T)(gk, c) = E(c, gk)
       }
     };
     fetch(0);
@@ -184,8 +184,8 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P
 #pragma unroll
       for (int u = 0; u < PER; u++) {
         const int idx = tid + u * FTHR;
-        as_w[idx] = (float)ra[u];
-        as_w[2 * FK * FB + idx] = (float)rb[u];
+        as_w[idx] = ra[u];
+        as_w[2 * FK * FB + idx] = rb[u];
       }
       __syncthreads();
       if (s + 1 < nslab) fetch((s + 1) * FK);
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           const int rr = lane + 32 * q;
-          if (c < LN && r0 + rr < m) P[(r0 + rr) + (i64)c * ldp] = (double)stage[cc * 129 + rr];
+          if (c < LN && r0 + rr < m) P[(r0 + rr) + (i64)c * ldp] = stage[cc * 129 + rr];
         }
       }
       __syncthreads();
@@ -240,12 +240,11 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(double* __restrict__ P
 // ---------------------------------------------------------------------------------
 // Diagonal tile of a reduced-precision factor, fused in one CTA and in FP32:
 //   L_jj = chol(D) (the dpotrf task, oocquark.cpp:87/393), X = L_jj^{-1},
-// written back as FP64: D's lower triangle := L_jj, E := X (lower, zeros above, ld lde),
-// Dinv := X^T (upper, zeros below, ld lde).  FP64 runs at ~7 GFLOP/s per SM on this part,
-// FP32 at 64x that; the tile's rounding (~1e-7) is below the trailing updates' own.
+// in place in the FP32 working matrix: D's lower triangle := L_jj, E := X (lower, zeros
+// above, ld lde), Dinv := X^T (upper, zeros below, ld lde).
 // Both phases are left-looking over 32-wide blocks, so every element is computed in
-// registers from finished data (L2-resident FP32 copies Lw, column-major, and Xr,
-// row-major, ld LN) and written once:
+// registers from finished data (D itself and Xr, a row-major FP32 scratch copy of X with
+// ld LN, both L2-resident) and written once:
 //   phase 1, block column K: C = A(K:, K) - L(K:, :K) L(K, :K)^T (thread per row, the
 //            32 L(K, :K) rows staged in shared memory), one warp factors C's 32 x 32 top
 //            in registers, one thread per row solves the rows below;
@@ -297,8 +296,7 @@ __device__ __forceinline__ void dg_dot32(float acc[DG_B], const float* __restric
 // S[q * 32 + c] = Lw(r0 + c, q) for q < nq, c < cb (0 for c >= cb): every load of the
 // thread is issued before the first store (a loop with one load per iteration would
 // wait an L2 round trip per element).
-__device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* __restrict__ Lw, i64 ldw, int r0,
-                                         int nq, int cb) {
+__device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* Lw, i64 ldw, int r0, int nq, int cb) {
   constexpr int PER = DG_MAX * DG_B / DG_THREADS;  // 32 elements per thread at most
   float v[PER];
 #pragma unroll
@@ -315,8 +313,8 @@ __device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* __r
 }
 
 __global__ void __launch_bounds__(DG_THREADS, 1)
-    k_diag_f32(double* __restrict__ D, i64 ldd, int LN, i64 col0, double* __restrict__ Dinv,
-               double* __restrict__ E, i64 lde, float* __restrict__ Lw, float* __restrict__ Xr, int* status) {
+    k_diag_f32(float* D, i64 ldd, int LN, i64 col0, float* __restrict__ Dinv, float* __restrict__ E, i64 lde,
+               float* __restrict__ Xr, int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(16) float dsm[];
   float* S = dsm;                      // staged rows, q-major: S[q * 32 + r]
@@ -326,7 +324,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
   float* dinv = Li + DG_B * DG_LD;     // 1 / L(k + c, k + c)
   __shared__ int s_fail;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const i64 ldw = LN;
+  float* Lw = D;  // L overwrites A in place
+  const i64 ldw = ldd;
+  const i64 ldx = LN;  // Xr
   if (t == 0) s_fail = 0;
   __syncthreads();
   // ---- phase 1: L = chol(D), block columns left to right
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
       const int i = k0 + t;
       float acc[DG_B];
 #pragma unroll
-      for (int c = 0; c < DG_B; c++) acc[c] = (c < kb && c <= t) ? (float)D[i + (i64)(k0 + c) * ldd] : 0.f;
+      for (int c = 0; c < DG_B; c++) acc[c] = (c < kb && c <= t) ? Lw[i + (i64)(k0 + c) * ldw] : 0.f;
       dg_dot32(acc, Lw + i, ldw, 0, k0, S, -1.f);
 #pragma unroll
       for (int c = 0; c < DG_B; c++) Cs[t * DG_LD + c] = acc[c];
@@ -393,10 +393,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
       }
 #pragma unroll
       for (int c = 0; c < DG_B; c++)
-        if (c < kb && c <= t) {
-          Lw[i + (k0 + c) * ldw] = row[c];
-          D[i + (i64)(k0 + c) * ldd] = (double)row[c];
-        }
+        if (c < kb && c <= t) Lw[i + (k0 + c) * ldw] = row[c];
     }
     __syncthreads();
   }
@@ -428,7 +425,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
       float acc[DG_B];
 #pragma unroll
       for (int r = 0; r < DG_B; r++) acc[r] = 0.f;
-      dg_dot32(acc, Xr + j, ldw, j, i0, S, 1.f);  // acc[r] = sum_q L(i0 + r, q) X(q, j)
+      dg_dot32(acc, Xr + j, ldx, j, i0, S, 1.f);  // acc[r] = sum_q L(i0 + r, q) X(q, j)
       float y[DG_B];
 #pragma unroll
       for (int r = 0; r < DG_B; r++) {
@@ -440,9 +437,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 #pragma unroll
       for (int r = 0; r < DG_B; r++)
         if (r < ib) {
-          Xr[(i0 + r) * ldw + j] = y[r];
-          E[(i0 + r) + (i64)j * lde] = (double)y[r];
-          Dinv[j + (i64)(i0 + r) * lde] = (double)y[r];
+          Xr[(i0 + r) * ldx + j] = y[r];
+          E[(i0 + r) + (i64)j * lde] = y[r];
+          Dinv[j + (i64)(i0 + r) * lde] = y[r];
         }
     } else if (t < LN) {
       const int c = t - i0;  // diagonal block column (c < ib) or right of it (zeros)
@@ -450,9 +447,9 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
       for (int r = 0; r < DG_B; r++)
         if (r < ib) {
           const float y = (c < ib && r >= c) ? Li[r * DG_LD + c] : 0.f;
-          if (c < ib) Xr[(i0 + r) * ldw + t] = y;
-          E[(i0 + r) + (i64)t * lde] = (double)y;
-          Dinv[t + (i64)(i0 + r) * lde] = (double)y;
+          if (c < ib) Xr[(i0 + r) * ldx + t] = y;
+          E[(i0 + r) + (i64)t * lde] = y;
+          Dinv[t + (i64)(i0 + r) * lde] = y;
         }
     }
     __syncthreads();
@@ -463,7 +460,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 __global__ void k_to_f32(const double* __restrict__ X, i64 ldx, float* __restrict__ Y, i64 ldy, int m, int K) {
   const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= m) return;
-  for (int k = blockIdx.y; k < K; k += gridDim.y) Y[r + k * ldy] = (float)X[r + k * ldx];
+  for (int k = blockIdx.y; k < K; k += gridDim.y) Y[r + k * ldy] = ooc_f64_to_f32(X[r + k * ldx]);
 }
 
 // ---------------------------------------------------------------------------------
@@ -660,11 +657,32 @@ __global__ void k_set_identity(T* D, i64 ld, int n) {
 }
 
 // Copy with conversion (column-major blocks).
+
+// Lower triangle (columns [c0, c0 + w), rows >= column) between the FP64 input/output and the
+// FP32 working matrix, converted on the integer pipe; `zero_upper` writes 0 above it.
+__device__ __forceinline__ float to_f32(double x) { return ooc_f64_to_f32(x); }
+__device__ __forceinline__ double to_f64(float x) { return ooc_f32_to_f64(x); }
 template <typename TS, typename TD>
-__global__ void k_copy_conv(const TS* __restrict__ S, i64 lds, TD* __restrict__ D, i64 ldd, int m, int n) {
+__global__ void k_lower_conv(const TS* __restrict__ S, i64 lds, TD* __restrict__ D, i64 ldd, i64 n, i64 c0, int w,
+                             int zero_upper) {
   const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= m) return;
-  for (int c = blockIdx.y; c < n; c += gridDim.y) D[r + (i64)c * ldd] = (TD)S[r + (i64)c * lds];
+  if (r >= n) return;
+  for (int cc = blockIdx.y; cc < w; cc += gridDim.y) {
+    const i64 c = c0 + cc;
+    if (r >= c) {
+      if constexpr (sizeof(TD) == 4) D[r + cc * ldd] = to_f32(S[r + cc * lds]);
+      else D[r + cc * ldd] = to_f64(S[r + cc * lds]);
+    } else if (zero_upper) {
+      D[r + cc * ldd] = TD(0);
+    }
+  }
+}
+// The uniform test matrix's lower triangle, rounded to FP32 (the same values as rounding
+// the FP64 generator's output).
+__global__ void k_gen_uniform_f32_lower(float* __restrict__ D, i64 ldd, i64 n, uint64_t key, double alpha) {
+  const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (i64 c = blockIdx.y; c <= r && c < n; c += gridDim.y) D[r + c * ldd] = ooc_uniform_elem_f32(key, n, alpha, r, c);
 }
 
 // x += d (columns), and per-column max |.| of x, r and b for the backward error.
@@ -703,38 +721,50 @@ __global__ void k_rowsum_abs(const double* A, i64 lda, int n, double* out) {
 // R(:, q) -= A(seed) X(:, q) over the columns [blockIdx.y * kslice, ...) of A, with A
 // regenerated element by element (uniform generator) instead of read from memory.
 // Partial sums per column slice go to P (nslice x m x r) for an ordered reduction.
+// The uniform test matrix's off-diagonal elements are integer multiples of 2^-54
+// (ooc_uniform_offdiag_int): the kernels below accumulate the integers and apply 2^-54 once
+// per row (a power of two commutes with rounding), one conversion per element.
+// P[slice](row, q) = sum over the slice's columns c of A(row, c) X(c, q), A regenerated.
+template <int R>
 __global__ void __launch_bounds__(256) k_resid_gen(uint64_t key, i64 n, double alpha, const double* __restrict__ X,
                                                    i64 ldx, int r, int kslice, double* __restrict__ P) {
-  __shared__ double Xs[NN_KCHUNK * RMAX];
+  __shared__ double Xs[NN_KCHUNK * R];
   const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   const int k0 = blockIdx.y * kslice;
   const int k1 = (int)min((i64)k0 + kslice, n);
-  double acc[RMAX];
+  double acc[R];  // in units of 2^-54
 #pragma unroll
-  for (int q = 0; q < RMAX; q++) acc[q] = 0;
+  for (int q = 0; q < R; q++) acc[q] = 0;
   for (int kc = k0; kc < k1; kc += NN_KCHUNK) {
     const int kn = min(NN_KCHUNK, k1 - kc);
     __syncthreads();
-    for (int idx = threadIdx.x; idx < kn * r; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
       const int q = idx / kn, kk = idx % kn;
-      Xs[kk * RMAX + q] = X[(kc + kk) + (i64)q * ldx];
+      Xs[kk * R + q] = (q < r) ? X[(kc + kk) + (i64)q * ldx] : 0.0;
     }
     __syncthreads();
     if (row < n) {
       for (int kk = 0; kk < kn; kk++) {
-        const double a = ooc_uniform_elem(key, n, alpha, row, kc + kk);
+        const i64 c = kc + kk;
+        const double a = (c == row) ? 0.0 : (double)ooc_uniform_offdiag_int(key, n, row, c);
 #pragma unroll
-        for (int q = 0; q < RMAX; q++)
-          if (q < r) acc[q] = fma(a, Xs[kk * RMAX + q], acc[q]);
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Xs[kk * R + q], acc[q]);
       }
     }
   }
   if (row >= n) return;
+  const bool has_diag = row >= k0 && row < k1;
+  const double aii = has_diag ? ooc_uniform_elem(key, n, alpha, row, row) : 0.0;
   double* Pz = P + (i64)blockIdx.y * n * r;
-  for (int q = 0; q < r; q++) Pz[row + (i64)q * n] = acc[q];
+  for (int q = 0; q < r; q++) {
+    double v = acc[q] * 0x1.0p-54;
+    if (has_diag) v = fma(aii, X[row + (i64)q * ldx], v);
+    Pz[row + (i64)q * n] = v;
+  }
 }
 
-// Partial row sums of |A(seed)| over column slices (P: nslice x n).
+// P[slice](row) = sum over the slice's columns of |A(row, c)|: integer sums of at most 512
+// terms (< 2^62), each converted once.
 __global__ void __launch_bounds__(256) k_rowsum_gen(uint64_t key, i64 n, double alpha, int kslice,
                                                     double* __restrict__ P) {
   const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -742,7 +772,18 @@ __global__ void __launch_bounds__(256) k_rowsum_gen(uint64_t key, i64 n, double 
   const int k0 = blockIdx.y * kslice;
   const int k1 = (int)min((i64)k0 + kslice, n);
   double s = 0;
-  for (int c = k0; c < k1; c++) s += fabs(ooc_uniform_elem(key, n, alpha, row, c));
+  for (int c0 = k0; c0 < k1; c0 += 512) {
+    const int c1 = min(k1, c0 + 512);
+    unsigned long long is = 0;
+    for (int c = c0; c < c1; c++) {
+      if (c == row) continue;
+      const long long v = ooc_uniform_offdiag_int(key, n, row, c);
+      is += (unsigned long long)(v < 0 ? -v : v);
+    }
+    s += (double)is;
+  }
+  s *= 0x1.0p-54;
+  if (row >= k0 && row < k1) s += fabs(ooc_uniform_elem(key, n, alpha, row, row));
   P[(i64)blockIdx.y * n + row] = s;
 }
 
@@ -770,6 +811,9 @@ __global__ void k_gen_normal(double* B, i64 ldb, i64 n, int r, uint64_t key) {
 int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status,
                        cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split,
                        int reserve_sms);
+int launch_syrk_bf16x3_f32(const float* X, i64 ldx, float* C, i64 ldc, int m, int K, const int* status,
+                           cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split,
+                           int reserve_sms);
 size_t bf16x3_work_bytes(int m, int K);
 
 namespace {
@@ -814,7 +858,7 @@ int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, 
     if (bj_lo >= hi) return OOC_OK;
     const i64 nblk = ooc_lower_blocks_before(hi, T) - ooc_lower_blocks_before(bj_lo, T);
     if (nblk > 0x7fffffff) return OOC_ERR_INTERNAL;
-    k_syrk_f32<<<(unsigned)nblk, FTHR, 0, s>>>(Y, ldy, C, ldc, m, K, (int)T, bj_lo, status);
+    k_syrk_f32<double><<<(unsigned)nblk, FTHR, 0, s>>>(Y, ldy, C, ldc, m, K, (int)T, bj_lo, status);
     OOC_CUDA_TRY(cudaGetLastError());
     return OOC_OK;
   }
@@ -825,6 +869,32 @@ int syrk_lowprec(int prec, const double* X, i64 ldx, double* C, i64 ldc, int m, 
     }
     return launch_syrk_bf16x3(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes, bj_lo, bj_hi, prepare,
                               reserve_sms);
+  }
+  return OOC_ERR_UNSUPPORTED;
+}
+
+// The same for the FP32 working matrix of a reduced-precision factor: C (FP32) -= X X^T
+// with X the FP32 column panel (no conversions).
+int syrk_f32(int prec, const float* X, i64 ldx, float* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
+             DevBuf& work, int bj_lo = 0, int bj_hi = -1, int prepare = 1, int reserve_sms = 0) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (prec == OOC_PREC_FP32) {
+    const i64 T = ((i64)m + FB - 1) / FB;
+    const i64 hi = std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
+    if (bj_lo >= hi) return OOC_OK;
+    const i64 nblk = ooc_lower_blocks_before(hi, T) - ooc_lower_blocks_before(bj_lo, T);
+    if (nblk > 0x7fffffff) return OOC_ERR_INTERNAL;
+    k_syrk_f32<float><<<(unsigned)nblk, FTHR, 0, s>>>(X, ldx, C, ldc, m, K, (int)T, bj_lo, status);
+    OOC_CUDA_TRY(cudaGetLastError());
+    return OOC_OK;
+  }
+  if (prec == OOC_PREC_BF16X3) {
+    if (prepare) {
+      int rc = work.ensure(bf16x3_work_bytes(m, K));
+      if (rc) return rc;
+    }
+    return launch_syrk_bf16x3_f32(X, ldx, C, ldc, m, K, status, s, work.p, work.bytes, bj_lo, bj_hi, prepare,
+                                  reserve_sms);
   }
   return OOC_ERR_UNSUPPORTED;
 }
@@ -944,9 +1014,12 @@ struct ooc_factor {
   i64 n = 0;
   int nb = 0;
   int prec = OOC_PREC_FP64;
+  // OOC_PREC_FP64: L and Dinv in FP64.  Reduced precision: the FP32 working matrix Lf is
+  // the factor (lower triangle; the strict upper triangle is not kept) and Dinvf its
+  // diagonal inverses; the FP64 members stay null.
   double* L = nullptr;     // n x n, ld n (owned); lower = factor
   double* Dinv = nullptr;  // bb tiles of nb x nb: L_JJ^{-T}
-  float* Lf = nullptr;     // FP32 copy of L, ld n
+  float* Lf = nullptr;     // n x n FP32, ld n
   float* Dinvf = nullptr;
   double* tmp = nullptr;   // nb x 16
   float* tmpf = nullptr;
@@ -966,23 +1039,21 @@ struct ooc_factor {
 
 namespace {
 
-int alloc_factor(ooc_factor* F, i64 n, int nb, bool want_f32) {
+int alloc_factor(ooc_factor* F, i64 n, int nb, bool reduced) {
   const int bb = (int)((n + nb - 1) / nb);
   const size_t tiles = (size_t)bb * nb * nb;
-  if (cudaMalloc(&F->L, (size_t)n * n * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&F->Dinv, tiles * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&F->tmp, (size_t)nb * RMAX * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&F->status, sizeof(int)) != cudaSuccess) {
+  bool ok = cudaMalloc(&F->status, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&F->tmp, (size_t)nb * RMAX * sizeof(double)) == cudaSuccess;
+  if (ok && !reduced)
+    ok = cudaMalloc(&F->L, (size_t)n * n * sizeof(double)) == cudaSuccess &&
+         cudaMalloc(&F->Dinv, tiles * sizeof(double)) == cudaSuccess;
+  if (ok && reduced)
+    ok = cudaMalloc(&F->Lf, (size_t)n * n * sizeof(float)) == cudaSuccess &&
+         cudaMalloc(&F->Dinvf, tiles * sizeof(float)) == cudaSuccess &&
+         cudaMalloc(&F->tmpf, (size_t)nb * RMAX * sizeof(float)) == cudaSuccess;
+  if (!ok) {
     cudaGetLastError();
     return OOC_ERR_NOMEM;
-  }
-  if (want_f32) {
-    if (cudaMalloc(&F->Lf, (size_t)n * n * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&F->Dinvf, tiles * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&F->tmpf, (size_t)nb * RMAX * sizeof(float)) != cudaSuccess) {
-      cudaGetLastError();
-      return OOC_ERR_NOMEM;
-    }
   }
   return OOC_OK;
 }
@@ -1001,23 +1072,14 @@ struct MixedProf {
   ~MixedProf() { for (cudaEvent_t e : ev) cudaEventDestroy(e); }
 };
 
-// Right-looking in-core factorization of F->L (ld n) with FP64 potrf and trailing updates
-// in `prec` (the reference's ooc_incore over the whole matrix, oocquark.cpp:389-419, with
-// the dsyrk/dgemm tasks as one lower-triangular update).
-//
-// The column solve B := B L_jj^{-T} runs as one product with the tile's inverse (kept for
-// the solves, formed in FP64 from the diagonal tile alone): for OOC_PREC_FP64 an FP64 DMMA
-// product B := W (L_jj^{-1})^T with W a copy of B, the triangular half of K skipped; for a
-// reduced-precision factor an FP32 product in place.
-//
-// Look-ahead on two streams.  FP64: the diagonal work of panel j (potrf, inverse, column
-// solve) runs on `s1` while `s0` performs the bulk of the trailing update of panel j-1.
-// Reduced precision: only potrf and inverse run on `s1` (latency-bound, few SMs; the
-// persistent tensor-core update leaves kChainSMs SMs free for them), the column solve
-// runs on `s0` with every SM.  In both, `s0` first updates only the next panel's block
-// columns and signals `s1`, then updates the rest.
-constexpr int kChainSMs = 8;
-
+// Right-looking in-core FP64 factorization of F->L (ld n) (the reference's ooc_incore over
+// the whole matrix, oocquark.cpp:389-419, with the dsyrk/dgemm tasks as one lower-
+// triangular update).  The column solve B := B L_jj^{-T} runs as one FP64 DMMA product
+// with the tile's inverse (kept for the solves, formed from the diagonal tile alone),
+// B := W (L_jj^{-1})^T with W a copy of B and the triangular half of K skipped.
+// Look-ahead on two streams: the diagonal work of panel j (potrf, inverse, column solve)
+// runs on `s1` while `s0` performs the bulk of the trailing update of panel j-1; `s0` first
+// updates only the next panel's columns and signals `s1`, then updates the rest.
 int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
@@ -1029,9 +1091,7 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
   if (rc) return rc;
   double* W = (double*)F->scratch.p;   // copy of the column panel (m x nb, ld n)
   double* E = W + (size_t)n * nb;      // L_jj^{-1} (lower, ld nb)
-  const bool split = (prec == OOC_PREC_FP64) || (nb % 128 == 0);
-  if (prec != OOC_PREC_FP64)  // per device: set on every call (cheap)
-    OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
+  (void)prec;
   cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: panel solved (s1 -> s0)
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evP, cudaEventDisableTiming));
@@ -1040,65 +1100,6 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
     ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
   } guard{evA, evP};
   OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
-  if (prec != OOC_PREC_FP64) {
-    for (int j = 0; j < bb; j++) {
-      const i64 J0 = (i64)j * nb;
-      const int LN = (int)std::min<i64>(nb, n - J0);
-      double* Djj = A + J0 + J0 * lda;
-      // ---- s1: FP64 diagonal tile and its inverse, beside the bulk update of panel j-1
-      OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
-      if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-      double* Dj = F->Dinv + (i64)j * tile;  // Dinv_j = L_jj^{-T}; E = Dinv_j^T = L_jj^{-1}
-      if (LN <= DG_MAX) {
-        // FP32 potrf + inverse in one CTA; working copies in the (here unused) panel scratch
-        float* Lw = (float*)W;
-        k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, Dj, E, nb, Lw, Lw + (size_t)LN * LN,
-                                                   F->status);
-        OOC_CUDA_TRY(cudaGetLastError());
-      } else {
-        rc = launch_potrf_tile(Djj, lda, LN, J0, F->status, s1);
-        if (rc) return rc;
-        k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s1>>>(Dj, nb, LN);
-        rc = launch_trsm_col(Djj, lda, TileCol{Dj, nb, tile}, 1, LN, LN, LN, F->status, s1);
-        if (rc) return rc;
-        k_transpose<<<dim3((LN + 31) / 32, (LN + 31) / 32), dim3(32, 8), 0, s1>>>(Dj, nb, E, nb, LN);
-      }
-      if (prof->on) prof->mark(s1);
-      OOC_CUDA_TRY(cudaEventRecord(evP, s1));
-      // ---- s0: column solve (FP32, in place), then the trailing update
-      OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
-      const i64 m = n - J0 - LN;
-      if (m > 0) {
-        double* Pn = Djj + LN;
-        if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
-        k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, E, nb, (int)m, LN, F->status);
-        OOC_CUDA_TRY(cudaGetLastError());
-        if (prof->on) {
-          prof->mark(s0);
-          prof->mark(s0);
-          prof->kind.push_back(1);
-          prof->flops.push_back((double)m * (double)(m + 1) * LN);
-        }
-        double* C = A + (J0 + LN) * (1 + lda);
-        if (split) {
-          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1, 0);
-          if (rc) return rc;
-          OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
-        } else {
-          rc = syrk_lowprec(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
-          if (rc) return rc;
-          OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-        }
-        if (rc) return rc;
-        if (prof->on) prof->mark(s0);
-      }
-      if (launches) *launches += 4 * ((LN + 63) / 64) + 8;
-    }
-    OOC_CUDA_TRY(cudaEventRecord(evP, s1));
-    OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
-    return OOC_OK;
-  }
   for (int j = 0; j < bb; j++) {
     const i64 J0 = (i64)j * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
@@ -1154,6 +1155,82 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
   return OOC_OK;
 }
 
+// Reduced-precision factorization of the FP32 working matrix F->Lf (ld n), right-looking
+// over nb-wide panels (nb <= 512):
+//   s1: the diagonal tile's Cholesky and inverse in one FP32 CTA (k_diag_f32), beside the
+//       bulk update of the previous panel (the persistent tensor-core update leaves
+//       kChainSMs SMs free for it);
+//   s0: the column solve (FP32 product with the inverse, in place, every SM), then the
+//       trailing update in `prec` -- the next panel's block columns first (an event lets
+//       s1 start on its diagonal tile), then the rest.
+constexpr int kChainSMs = 8;
+
+int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
+  const i64 n = F->n;
+  const int nb = F->nb;
+  const int bb = (int)((n + nb - 1) / nb);
+  float* A = F->Lf;
+  const i64 lda = n;
+  const i64 tile = (i64)nb * nb;
+  if (nb > DG_MAX) return OOC_ERR_UNSUPPORTED;
+  int rc = F->scratch.ensure((size_t)2 * tile * sizeof(float));
+  if (rc) return rc;
+  float* E = (float*)F->scratch.p;  // L_jj^{-1} (lower, ld nb)
+  float* Xr = E + tile;             // row-major copy for the diagonal kernel
+  const bool split = (nb % 128 == 0);
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
+  cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: diagonal tile done (s1 -> s0)
+  OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
+  OOC_CUDA_TRY(cudaEventCreateWithFlags(&evP, cudaEventDisableTiming));
+  struct EvGuard {
+    cudaEvent_t a, b;
+    ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+  } guard{evA, evP};
+  OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
+  for (int j = 0; j < bb; j++) {
+    const i64 J0 = (i64)j * nb;
+    const int LN = (int)std::min<i64>(nb, n - J0);
+    float* Djj = A + J0 + J0 * lda;
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
+    if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
+    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, E, nb, Xr, F->status);
+    OOC_CUDA_TRY(cudaGetLastError());
+    if (prof->on) prof->mark(s1);
+    OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+    const i64 m = n - J0 - LN;
+    if (m > 0) {
+      float* Pn = Djj + LN;
+      if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
+      k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, E, nb, (int)m, LN, F->status);
+      OOC_CUDA_TRY(cudaGetLastError());
+      if (prof->on) {
+        prof->mark(s0);
+        prof->mark(s0);
+        prof->kind.push_back(1);
+        prof->flops.push_back((double)m * (double)(m + 1) * LN);
+      }
+      float* C = A + (J0 + LN) * (1 + lda);
+      if (split) {
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1, 0);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
+      } else {
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+      }
+      if (rc) return rc;
+      if (prof->on) prof->mark(s0);
+    }
+    if (launches) *launches += 5;
+  }
+  OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+  OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+  return OOC_OK;
+}
+
 int read_int(const int* d, int* h, cudaStream_t s) {
   OOC_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
   OOC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1168,8 +1245,9 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   if (!gen && !A && n > 0) return -2;
   if (n <= 0) return -3;
   if (!gen && lda < n) return -4;
-  if (nb <= 0) return -5;
   if (prec != OOC_PREC_FP64 && prec != OOC_PREC_FP32 && prec != OOC_PREC_BF16X3) return -6;
+  const bool reduced = prec != OOC_PREC_FP64;
+  if (nb <= 0 || (reduced && nb > DG_MAX)) return -5;
   if (!out) return -7;
   if (!info) return -8;
   *out = nullptr;
@@ -1182,21 +1260,51 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   F->n = n;
   F->nb = nb;
   F->prec = prec;
-  int rc = alloc_factor(F, n, nb, prec != OOC_PREC_FP64);
+  int rc = alloc_factor(F, n, nb, reduced);
   if (rc) { delete F; return rc; }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  // copy A (host or device) into the factor's storage
+  // A (generated, host or device) into the factor's storage
   rc = OOC_OK;
   if (cudaMemsetAsync(F->status, 0, sizeof(int), s) != cudaSuccess) rc = OOC_ERR_CUDA;
-  if (!rc) {
+  if (!rc && !reduced) {
     if (gen) {
       rc = launch_gen_uniform_block(F->L, n, n, seed, alpha, 0, 0, n, n, s);
     } else if (cudaMemcpy2DAsync(F->L, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDefault, s) != cudaSuccess) {
       rc = OOC_ERR_CUDA;
     }
+  } else if (!rc) {
+    const unsigned gx = (unsigned)((n + 255) / 256);
+    if (gen) {
+      k_gen_uniform_f32_lower<<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256, 0, s>>>(
+          F->Lf, n, n, ooc_uniform_key(seed), alpha);
+    } else {
+      cudaPointerAttributes pa{};
+      const bool on_device = cudaPointerGetAttributes(&pa, A) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+      cudaGetLastError();
+      if (on_device) {
+        k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256, 0, s>>>(A, lda, F->Lf, n, n,
+                                                                                             0, (int)n, 0);
+      } else {  // host matrix: column blocks through a staging buffer
+        const int w = (int)std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
+        DevBuf stage;
+        rc = stage.ensure((size_t)n * w * sizeof(double));
+        for (i64 c0 = 0; !rc && c0 < n; c0 += w) {
+          const int wc = (int)std::min<i64>(w, n - c0);
+          if (cudaMemcpy2DAsync(stage.p, n * sizeof(double), A + c0 * lda, lda * sizeof(double), n * sizeof(double), wc,
+                                cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            rc = OOC_ERR_CUDA;
+            break;
+          }
+          k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min(wc, 1024)), 256, 0, s>>>(
+              (const double*)stage.p, n, F->Lf + c0 * n, n, n, c0, wc, 0);
+        }
+        if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = OOC_ERR_CUDA;  // before the staging buffer goes
+      }
+    }
+    if (!rc && cudaGetLastError() != cudaSuccess) rc = OOC_ERR_CUDA;
   }
   int64_t launches = 0;
   MixedProf prof;
@@ -1209,14 +1317,8 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     cudaEventRecord(e0, s);
     void* s1p = nullptr;
     ooc_get_stream(h, 1, &s1p);
-    rc = factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);
-    if (!rc && F->Lf) {
-      const int bb = (int)((n + nb - 1) / nb);
-      k_copy_conv<double, float><<<dim3((unsigned)((n + 255) / 256), 1024), 256, 0, s>>>(F->L, n, F->Lf, n, (int)n,
-                                                                                         (int)n);
-      k_copy_conv<double, float><<<dim3((unsigned)((nb + 255) / 256), 1024), 256, 0, s>>>(
-          F->Dinv, nb, F->Dinvf, nb, nb, bb * nb);
-    }
+    rc = reduced ? factor_f32(F, prec, s, (cudaStream_t)s1p, &launches, &prof)
+                 : factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);
     cudaEventRecord(e1, s);
   }
   int st = 0;
@@ -1265,10 +1367,10 @@ extern "C" int ooc_factor_create_gen(ooc_handle* h, int64_t n, uint64_t seed, do
 extern "C" int64_t ooc_factor_bytes(int64_t n, int nb, int prec) {
   if (n <= 0 || nb <= 0) return 0;
   const int64_t bb = (n + nb - 1) / nb;
-  int64_t b = n * n * 8 + bb * nb * nb * 8 + (int64_t)nb * 16 * 8 + n * nb * 8 + (int64_t)nb * nb * 8;
-  if (prec != OOC_PREC_FP64) b += n * n * 4 + bb * nb * nb * 4 + (int64_t)nb * 16 * 4;
-  if (prec == OOC_PREC_BF16X3) b += 2 * ((n + 127) / 128 * 128) * ((nb + 63) / 64 * 64) * 2;
-  if (prec == OOC_PREC_FP32) b += ((n + 3) / 4 * 4) * nb * 4;
+  int64_t b = (int64_t)nb * 16 * 8 + 256;  // tmp, status
+  if (prec == OOC_PREC_FP64) return b + n * n * 8 + bb * nb * nb * 8 + n * nb * 8 + (int64_t)nb * nb * 8;
+  b += n * n * 4 + bb * nb * nb * 4 + (int64_t)nb * 16 * 4 + 2 * (int64_t)nb * nb * 4;  // Lf, Dinvf, tmpf, scratch
+  if (prec == OOC_PREC_BF16X3) b += 2 * ((n + 127) / 128 * 128) * ((nb + 63) / 64 * 64) * 2;  // split planes
   return b;
 }
 
@@ -1283,46 +1385,26 @@ extern "C" int ooc_factor_destroy(ooc_factor* F) {
   return OOC_OK;
 }
 
-extern "C" int ooc_factor_copy_L(ooc_factor* F, double* L, int64_t ldl) {
-  if (!F) return -1;
-  if (!L) return -2;
-  if (ldl < F->n) return -3;
-  cudaSetDevice(F->device);
-  OOC_CUDA_TRY(cudaMemcpy2D(L, ldl * sizeof(double), F->L, F->n * sizeof(double), F->n * sizeof(double), F->n,
-                            cudaMemcpyDefault));
-  return OOC_OK;
-}
-
-// Plain solve with the factor (FP64 triangular solves): B := A^{-1} B, B on the device.
-extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t ldb, int nrhs) {
-  if (!h) return -1;
-  if (!F) return -2;
-  if (!B) return -3;
-  if (ldb < F->n) return -4;
-  if (nrhs < 0 || nrhs > RMAX) return -5;
-  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
-  cudaSetDevice(F->device);
-  cudaStream_t s = ooc_compute_stream(h);
-  int rc = solve_with<double>(F->L, F->n, F->Dinv, F->n, F->nb, B, ldb, nrhs, F->tmp, s, &F->part);
-  if (rc) return rc;
-  return ooc_wait_stream(h, s);
-}
-
 namespace {
 __global__ void k_residual_init(const double* B, i64 ldb, double* R, i64 ldr, int n, int r) {
   const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   for (int q = 0; q < r; q++) R[i + q * ldr] = B[i + q * ldb];
 }
+__global__ void k_f32_to_f64_cols(const float* S, i64 lds, double* D, i64 ldd, int n, int r) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) D[i + q * ldd] = ooc_f32_to_f64(S[i + q * lds]);
+}
 __global__ void k_to_f32_cols(const double* S, i64 lds, float* D, i64 ldd, int n, int r) {
   const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  for (int q = 0; q < r; q++) D[i + q * ldd] = (float)S[i + q * lds];
+  for (int q = 0; q < r; q++) D[i + q * ldd] = ooc_f64_to_f32(S[i + q * lds]);
 }
 __global__ void k_add_f32_cols(double* X, i64 ldx, const float* D, i64 ldd, int n, int r) {
   const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  for (int q = 0; q < r; q++) X[i + q * ldx] += (double)D[i + q * ldd];
+  for (int q = 0; q < r; q++) X[i + q * ldx] += ooc_f32_to_f64(D[i + q * ldd]);
 }
 
 double host_max(const std::vector<double>& v, int r, int q, int nb) {
@@ -1331,6 +1413,76 @@ double host_max(const std::vector<double>& v, int r, int q, int nb) {
   return m;
 }
 }  // namespace
+
+extern "C" int ooc_factor_copy_L(ooc_factor* F, double* L, int64_t ldl) {
+  if (!F) return -1;
+  if (!L) return -2;
+  if (ldl < F->n) return -3;
+  cudaSetDevice(F->device);
+  const i64 n = F->n;
+  if (!F->Lf) {
+    OOC_CUDA_TRY(cudaMemcpy2D(L, ldl * sizeof(double), F->L, n * sizeof(double), n * sizeof(double), n,
+                              cudaMemcpyDefault));
+    return OOC_OK;
+  }
+  // reduced precision: the FP32 factor widened to FP64, zeros above the diagonal, through a
+  // staging buffer of column blocks
+  cudaPointerAttributes pa{};
+  const bool on_device = cudaPointerGetAttributes(&pa, L) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  const unsigned gx = (unsigned)((n + 255) / 256);
+  if (on_device) {
+    k_lower_conv<float, double><<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256>>>(F->Lf, n, L, ldl, n, 0, (int)n, 1);
+    OOC_CUDA_TRY(cudaGetLastError());
+    OOC_CUDA_TRY(cudaDeviceSynchronize());
+    return OOC_OK;
+  }
+  const int w = (int)std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
+  DevBuf stage;
+  int rc = stage.ensure((size_t)n * w * sizeof(double));
+  if (rc) return rc;
+  for (i64 c0 = 0; c0 < n; c0 += w) {
+    const int wc = (int)std::min<i64>(w, n - c0);
+    k_lower_conv<float, double><<<dim3(gx, (unsigned)std::min(wc, 1024)), 256>>>(F->Lf + c0 * n, n, (double*)stage.p, n,
+                                                                                 n, c0, wc, 1);
+    OOC_CUDA_TRY(cudaGetLastError());
+    OOC_CUDA_TRY(cudaMemcpy2D(L + c0 * ldl, ldl * sizeof(double), stage.p, n * sizeof(double), n * sizeof(double), wc,
+                              cudaMemcpyDeviceToHost));
+  }
+  return OOC_OK;
+}
+
+// Plain solve with the factor: B := A^{-1} B, B on the device (FP64 triangular solves; for a
+// reduced-precision factor the solves run in FP32 on a rounded copy of B).
+extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t ldb, int nrhs) {
+  if (!h) return -1;
+  if (!F) return -2;
+  if (!B) return -3;
+  if (ldb < F->n) return -4;
+  if (nrhs < 0 || nrhs > RMAX) return -5;
+  if (F->info != 0) return OOC_ERR_UNSUPPORTED;
+  if (nrhs == 0) return OOC_OK;
+  cudaSetDevice(F->device);
+  cudaStream_t s = ooc_compute_stream(h);
+  const i64 n = F->n;
+  int rc;
+  if (F->Lf) {
+    DevBuf bf;
+    rc = bf.ensure((size_t)n * nrhs * sizeof(float));
+    if (rc) return rc;
+    const unsigned gb = (unsigned)((n + 255) / 256);
+    k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, (float*)bf.p, n, (int)n, nrhs);
+    rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, (float*)bf.p, n, nrhs, F->tmpf, s, &F->partf);
+    if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>((const float*)bf.p, n, B, ldb, (int)n, nrhs);
+    if (!rc) rc = ooc_wait_stream(h, s);  // before the staging buffer goes
+    return rc;
+  }
+  rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, B, ldb, nrhs, F->tmp, s, &F->part);
+  if (rc) return rc;
+  return ooc_wait_stream(h, s);
+}
+
+
 
 // Iterative refinement to a normwise backward error <= tol: X0 from the factor in FP64,
 // then repeat R = B - A X (FP64), D = A_F^{-1} R with the factor (FP32 copy for a
@@ -1388,7 +1540,11 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   }
   std::vector<double> nb_(r), nx(r), nr(r);
   if (!rc) rc = colmax(B, ldb, r, nb_);
-  if (!rc) {
+  if (!rc && F->Lf) {  // X0 from the FP32 factor
+    k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, Rf, n, (int)n, r);
+    rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+    if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>(Rf, n, X, ldx, (int)n, r);
+  } else if (!rc) {
     OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
                                    cudaMemcpyDeviceToDevice, s));
     rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, X, ldx, r, F->tmp, s, &F->part);
@@ -1401,7 +1557,8 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     if (gen) {
       rc = F->part.ensure((size_t)gslices * n * r * sizeof(double));
       if (rc) break;
-      k_resid_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, X, ldx, r, gks, (double*)F->part.p);
+      NN_DISPATCH(r, (k_resid_gen<RR><<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, X, ldx, r, gks,
+                                                                         (double*)F->part.p)));
       k_reduce_slices<double><<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, R, n, (int)n, r, -1.0, 1.0);
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) { ooc_set_last_error(e, "generated residual", __FILE__, __LINE__); rc = OOC_ERR_CUDA; break; }

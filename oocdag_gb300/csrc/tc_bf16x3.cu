@@ -115,24 +115,32 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
 }
 
 // ------------------------------------ kernels ------------------------------------
-// Split: X (m x K FP64, column-major) -> hi/lo planes (Mp x Kp BF16, row-major, zero pad).
-__global__ void k_split_bf16(const double* __restrict__ X, i64 ldx, __nv_bfloat16* __restrict__ hi,
+// Split: X (m x K, FP64 or FP32, column-major) -> hi/lo planes (Mp x Kp BF16, row-major,
+// zero pad).  FP32 input stays on the FP32 pipe (x - hi is exact in FP32).
+template <typename TX>
+__global__ void k_split_bf16(const TX* __restrict__ X, i64 ldx, __nv_bfloat16* __restrict__ hi,
                              __nv_bfloat16* __restrict__ lo, int m, int K, int Mp, int Kp) {
-  __shared__ double t[32][33];
+  __shared__ TX t[32][33];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   // read 32 x 32 (rows r0.., cols k0..) coalesced along rows
   for (int c = threadIdx.y; c < 32; c += blockDim.y) {
     const int r = r0 + threadIdx.x, k = k0 + c;
-    t[c][threadIdx.x] = (r < m && k < K) ? X[r + (i64)k * ldx] : 0.0;
+    t[c][threadIdx.x] = (r < m && k < K) ? X[r + (i64)k * ldx] : TX(0);
   }
   __syncthreads();
   // write rows, coalesced along k
   for (int rr = threadIdx.y; rr < 32; rr += blockDim.y) {
     const int r = r0 + rr, k = k0 + threadIdx.x;
     if (r < Mp && k < Kp) {
-      const double x = t[threadIdx.x][rr];
-      const __nv_bfloat16 h = __double2bfloat16(x);
-      const __nv_bfloat16 l = __double2bfloat16(x - (double)__bfloat162float(h));
+      const TX x = t[threadIdx.x][rr];
+      __nv_bfloat16 h, l;
+      if constexpr (sizeof(TX) == 4) {
+        h = __float2bfloat16_rn(x);
+        l = __float2bfloat16_rn(x - __bfloat162float(h));
+      } else {
+        h = __double2bfloat16(x);
+        l = __double2bfloat16(x - (double)__bfloat162float(h));
+      }
       hi[(i64)r * Kp + k] = h;
       lo[(i64)r * Kp + k] = l;
     }
@@ -151,7 +159,7 @@ __device__ __forceinline__ void strip_block_decode(i64 t, int T, int bj_lo, int 
     if (t < cnt) {
       int r, c;
       if (t < tri) {
-        r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);  // t < 136: exact enough, corrected below
         while ((i64)(r + 1) * (r + 2) / 2 <= t) r++;
         while ((i64)r * (r + 1) / 2 > t) r--;
         c = (int)(t - (i64)r * (r + 1) / 2);
@@ -169,9 +177,10 @@ __device__ __forceinline__ void strip_block_decode(i64 t, int T, int bj_lo, int 
   *bi = *bj = 0;  // not reached for t < number of blocks
 }
 
+template <typename TC>
 __global__ void __launch_bounds__(THREADS, 1)
     k_syrk_bf16x3(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
-                  double* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
+                  TC* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
                   int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -293,16 +302,16 @@ __global__ void __launch_bounds__(THREADS, 1)
     int tl = 0;
     i64 t = blockIdx.x;
     int bi = 0, bj = 0;
-    double cv[32];
+    TC cv[32];
     if (t < nblk) strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
     {
       const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
       const bool diag = (bi == bj);
-      const double* base = C + row + (i64)c0 * ldc;
+      const TC* base = C + row + (i64)c0 * ldc;
 #pragma unroll
       for (int q = 0; q < 32; q++) {
         const int col = c0 + q;
-        cv[q] = (t < nblk && row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
+        cv[q] = (t < nblk && row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : TC(0);
       }
     }
     for (; t < nblk; t += gridDim.x, tl++) {
@@ -318,7 +327,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * TB + cq);
       const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
       const bool diag = (bi == bj);
-      double* base = C + row + (i64)c0 * ldc;
+      TC* base = C + row + (i64)c0 * ldc;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         uint32_t v[16];
@@ -338,7 +347,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           for (int q = 0; q < 16; q++) {
             const int col = c0 + 16 * h + q;
             if (col < m && (!diag || col <= row))
-              base[(i64)(16 * h + q) * ldc] = cv[16 * h + q] - (double)__uint_as_float(v[q]);
+              base[(i64)(16 * h + q) * ldc] = cv[16 * h + q] - (TC)__uint_as_float(v[q]);
           }
         }
       }
@@ -347,11 +356,11 @@ __global__ void __launch_bounds__(THREADS, 1)
         strip_block_decode(tn, T, bj_lo, bj_hi, &bi, &bj);
         const int row = bi * TB + quad * 32 + lane, c0 = bj * TB + cq;
         const bool diag = (bi == bj);
-        const double* base = C + row + (i64)c0 * ldc;
+        const TC* base = C + row + (i64)c0 * ldc;
 #pragma unroll
         for (int q = 0; q < 32; q++) {
           const int col = c0 + q;
-          cv[q] = (row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : 0.0;
+          cv[q] = (row < m && col < m && (!diag || col <= row)) ? base[(i64)q * ldc] : TC(0);
         }
       }
     }
@@ -414,8 +423,10 @@ size_t bf16x3_work_bytes(int m, int K) {
   return 2 * Mp * Kp * sizeof(__nv_bfloat16) + 256;
 }
 
-int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
-                       void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split, int reserve_sms) {
+namespace {
+template <typename TX, typename TC>
+int launch_syrk_t(const TX* X, i64 ldx, TC* C, i64 ldc, int m, int K, const int* status, cudaStream_t s, void* work,
+                  size_t work_bytes, int bj_lo, int bj_hi, int do_split, int reserve_sms) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (!status) return OOC_ERR_INTERNAL;
   int rc = get_encode();
@@ -427,7 +438,7 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
   __nv_bfloat16* lo = hi + (size_t)Mp * Kp;
   if (do_split) {
     dim3 sg((unsigned)(Kp / 32), (unsigned)(Mp / 32));
-    k_split_bf16<<<sg, dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp, Kp);
+    k_split_bf16<TX><<<sg, dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp, Kp);
     OOC_CUDA_TRY(cudaGetLastError());
   }
   CUtensorMap mh, ml;
@@ -436,7 +447,7 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
     return OOC_ERR_CUDA;
   }
   // per device: set on every launch (cheap)
-  OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
   const i64 T = Mp / TB;
   bj_hi = (int)std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
   if (bj_lo >= bj_hi) return OOC_OK;
@@ -445,8 +456,23 @@ int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int 
   OOC_CUDA_TRY(cudaGetDevice(&dev));
   OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const i64 grid = std::max<i64>(1, std::min<i64>(nblk, std::max(1, nsm - std::max(0, reserve_sms))));
-  k_syrk_bf16x3<<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo, bj_hi, nblk,
+  k_syrk_bf16x3<TC><<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo, bj_hi, nblk,
                                                             const_cast<int*>(status));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
+}
+}  // namespace
+
+int launch_syrk_bf16x3(const double* X, i64 ldx, double* C, i64 ldc, int m, int K, const int* status, cudaStream_t s,
+                       void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split, int reserve_sms) {
+  return launch_syrk_t<double, double>(X, ldx, C, ldc, m, K, status, s, work, work_bytes, bj_lo, bj_hi, do_split,
+                                       reserve_sms);
+}
+
+// FP32 trailing matrix (reduced-precision factors): C (FP32) -= X X^T, X FP32.
+int launch_syrk_bf16x3_f32(const float* X, i64 ldx, float* C, i64 ldc, int m, int K, const int* status,
+                           cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split,
+                           int reserve_sms) {
+  return launch_syrk_t<float, float>(X, ldx, C, ldc, m, K, status, s, work, work_bytes, bj_lo, bj_hi, do_split,
+                                     reserve_sms);
 }

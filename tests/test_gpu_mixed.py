@@ -178,3 +178,20 @@ def test_generated_factor_and_refinement(oracle_mod, handle, prec):
     assert abs(B.mean()) < 0.1 and 0.9 < B.std() < 1.1  # the N(0,1) generator
     Fg.close()
     Fs.close()
+
+
+def test_reduced_factor_keeps_only_fp32(oracle_mod, handle, ooc):
+    # A reduced-precision factor is the FP32 working matrix (half the FP64 factor's memory,
+    # no FP64 copy); copy_L widens it exactly (every value an FP32 number), zeros above.
+    n, nb = 1100, 256
+    assert ooc.factor_bytes(65536, 512, "bf16x3") < 0.51 * ooc.factor_bytes(65536, 512, "fp64")
+    A, alpha = _c2_matrix(oracle_mod, n, 0.1)
+    with handle.factor(A, n, n, nb, "bf16x3") as F:
+        L = np.asfortranarray(np.full((n, n), np.nan))
+        F.copy_L(L, n)
+    assert np.all(np.triu(L, 1) == 0)
+    low = np.tril(L)
+    np.testing.assert_array_equal(low.astype(np.float32).astype(np.float64), low)
+    Lo = A.copy(order="F")
+    oracle_mod.cholesky(Lo, nb, 1 << 30, 4, 2)
+    assert np.abs(low - np.tril(Lo)).max() <= 1e-3 * np.abs(np.tril(Lo)).max()
