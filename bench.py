@@ -139,13 +139,19 @@ def barrier(world):
         dist.barrier()
 
 
+def _reduce_device() -> str:
+    import torch.distributed as dist
+
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def allreduce_max(x: float, world: int) -> float:
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -156,7 +162,7 @@ def allreduce_sum(x: float, world: int) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
@@ -501,6 +507,7 @@ def run_mixed(args):
         fp64 = {"value": flops / t64 / 1e12, "unit": "TFLOP/s", "ms_per_step": t64 * 1e3, "steps": 1,
                 "warmup": 0, "backward_error": be64, "factor_seconds": st64["seconds"],
                 "note": "plain FP64 path (DMMA updates, FP64 solve), same A and b, measured once",
+                "fp64_dmma_peak_tflops": fp64_peak, "frac_of_fp64_peak": (flops / t64 / 1e12) / fp64_peak,
                 "speedup_mixed_over_fp64": (value / world) / (flops / t64 / 1e12)}
 
     # ---- errors of every solve form, per delta (untimed) --------------------------------
@@ -559,31 +566,39 @@ def run_mixed(args):
         del Ah, Bh, Xh, Ad, Bd, Xd
 
     # ---- roofline of the dominant kernel ------------------------------------------------
+    # Trailing update of panel j (m = n - (j+1) nb rows below it, K = nb): algorithmic
+    # m (m+1) K useful flops, three BF16 tensor products of each (hi*hi, hi*lo, lo*hi); bytes:
+    # the FP32 lower triangle read and written (8 B per element), the FP32 panel read by the
+    # split (4 B per element) and the two BF16 planes written and read once (8 B per element).
     upd_bytes = 0.0
-    # C lower read + written once per update (16 B per element) plus the FP64 panel read
-    # and the two BF16 planes written and read (12 B per panel element).
     for j in range(n // nb - 1):
         m = n - (j + 1) * nb
-        upd_bytes += m * (m + 1) / 2 * 16 + m * nb * (8 + 4 * 2)
+        upd_bytes += m * (m + 1) / 2 * 8 + m * nb * (4 + 8)
     upd_bytes *= args.steps
     share_upd = upd_ms / (ms_local * args.steps)
     share_fac = fac_ms / (ms_local * args.steps)
-    upd_roof = {"kernel": f"k_syrk_{args.prec} (split-BF16 tcgen05 trailing update)" if args.prec == "bf16x3"
-                else "k_syrk_f32 (FP32 trailing update)",
-                "bound": "hbm", "achieved": upd_bytes / (upd_ms / 1e3) / 1e9 if upd_ms else None,
-                "peak": hbm_peak, "unit": "GB/s", "launches": upd_launch,
-                "avg_launch_ms": upd_ms / max(1, upd_launch), "share_of_step": share_upd,
-                "tensor_tflops": 3 * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-    if upd_roof["achieved"] and hbm_peak:
-        upd_roof["frac"] = upd_roof["achieved"] / hbm_peak
-    trsm_flops = sum((n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
-    fac_roof = {"kernel": "FP64 diagonal potrf + inverse + column solve (DMMA)", "bound": "fp64-dmma",
-                "achieved": trsm_flops / (fac_ms / 1e3) / 1e12 if fac_ms else None, "peak": fp64_peak,
+    bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
+    mult = 3 if args.prec == "bf16x3" else 1
+    upd_roof = {"kernel": "k_syrk_bf16x3<float> (persistent split-BF16 tcgen05 trailing update, FP32 C)"
+                if args.prec == "bf16x3" else "k_syrk_f32<float> (FP32 FFMA trailing update)",
+                "bound": "tensor" if args.prec == "bf16x3" else "fp32-simt",
+                "achieved": mult * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
+                "peak": bf16_peak if args.prec == "bf16x3" else None, "unit": "TFLOP/s",
+                "launches": upd_launch, "avg_launch_ms": upd_ms / max(1, upd_launch), "share_of_step": share_upd,
+                "algorithmic_flops_per_launch": mult * upd_flops / max(1, upd_launch),
+                "dram_gbs_algorithmic": upd_bytes / (upd_ms / 1e3) / 1e9 if upd_ms else None,
+                "hbm_peak_gbs": hbm_peak,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured; the kernel runs inside a "
+                               "seconds-long step)"}
+    if upd_roof["achieved"] and upd_roof["peak"]:
+        upd_roof["frac"] = upd_roof["achieved"] / upd_roof["peak"]
+    chain_flops = sum(2 * nb ** 3 / 3 + (n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
+    fac_roof = {"kernel": "diagonal chain: k_diag_f32 (FP32 potrf + inverse of the 512x512 tile, one CTA) + "
+                          "k_colsolve_f32 (FP32 column solve)",
+                "bound": "latency (one CTA) / fp32-simt",
+                "achieved": chain_flops / (fac_ms / 1e3) / 1e12 if fac_ms else None, "peak": None,
                 "unit": "TFLOP/s", "share_of_step": share_fac,
-                "peak_source": "measured live: FP64 DMMA issue loop (ooc_fp64_peak_probe)"}
-    if fac_roof["achieved"]:
-        fac_roof["frac"] = fac_roof["achieved"] / fp64_peak
+                "note": "segments on two streams overlap the update; share is their summed device time"}
     dominant, other = (upd_roof, fac_roof) if share_upd >= share_fac else (fac_roof, upd_roof)
     roofline = dict(dominant)
     roofline["traffic"] = None

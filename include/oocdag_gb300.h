@@ -88,6 +88,14 @@ int ooc_get_stream(ooc_handle* h, int which, void** stream);
 int ooc_dpotrf_L(ooc_handle* h, double* A, int64_t n, int64_t lda, int nb, size_t dev_budget,
                  int* info, ooc_stats* stats);
 
+/* FP32 Cholesky A = L L^T in place (lower; upper triangle untouched).  The reference has
+ * no FP32 entry (LIN/psmatgen.f exists but nothing binds it).  A on the device: factored
+ * in place (FP32 diagonal tiles, column solves and FP32 trailing updates, nb <= 512).
+ * A on the host: factored on a device copy, which must fit in dev_budget bytes (0 = 3/4
+ * of free device memory), else OOC_ERR_BUDGET.  *info as for ooc_dpotrf_L.            */
+int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int nb, size_t dev_budget,
+                 int* info, ooc_stats* stats);
+
 /* Drop-in for the reference driver entry (oocdag.cpp:18): same argument order, the
  * QUARK context replaced by an ooc_handle (NULL = a per-process handle on the current
  * device).  Returns the factorization time in seconds, or a negative status code.  */

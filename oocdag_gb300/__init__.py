@@ -112,6 +112,7 @@ def load(build_if_missing: bool = True):
     L.ooc_last_error_string.restype = ctypes.c_char_p
     L.ooc_last_info.argtypes = [P]
     L.ooc_dpotrf_L.argtypes = [P, P, I64, I64, I, SZ, ctypes.POINTER(I), ctypes.POINTER(OocStats)]
+    L.ooc_spotrf_L.argtypes = [P, P, I64, I64, I, SZ, ctypes.POINTER(I), ctypes.POINTER(OocStats)]
     L.Cholesky.argtypes = [P, P, I, I, I, SZ]
     L.Cholesky.restype = D
     L.ooc_pdpotrf_.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), ctypes.POINTER(I),
@@ -247,6 +248,16 @@ class Handle:
         self._after_torch(A)
         rc = load().ooc_dpotrf_L(self._h, _ptr(A), n, lda, nb, budget, ctypes.byref(info), ctypes.byref(st))
         _check(rc, "ooc_dpotrf_L")
+        return Result(info.value, st.as_dict())
+
+    def spotrf_L(self, A, n: int, lda: int, nb: int, budget: int = 0) -> Result:
+        """FP32 lower Cholesky in place (device A: in place; host A: on a device copy that
+        must fit in `budget` bytes, 0 = 3/4 of free memory)."""
+        info = ctypes.c_int(0)
+        st = OocStats()
+        self._after_torch(A)
+        rc = load().ooc_spotrf_L(self._h, _ptr(A), n, lda, nb, budget, ctypes.byref(info), ctypes.byref(st))
+        _check(rc, "ooc_spotrf_L")
         return Result(info.value, st.as_dict())
 
     def matgen_uniform(self, A, n: int, lda: int, seed: int, alpha: float) -> None:

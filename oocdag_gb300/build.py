@@ -1,8 +1,9 @@
 """Build recipe for the CUDA library (sm_103a only).
 
 Compiles every ``csrc/*.cu`` translation unit with nvcc in parallel and links them into
-``oocdag_gb300/_build/liboocdag_gb300.so`` (in-tree; git-ignored).  No cmake, no torch
-extension machinery: the library is a plain C-ABI shared object.
+``oocdag_gb300/_build/liboocdag_gb300.so`` (in-tree; git-ignored), then the command-line
+driver ``_build/oocdag`` (``csrc/oocdag_main.cpp``, host C++ against the C-ABI only).  No
+cmake, no torch extension machinery: the library is a plain C-ABI shared object.
 """
 from __future__ import annotations
 
@@ -17,6 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboocdag_gb300.so")
+CLI = os.path.join(BUILD, "oocdag")
+CLI_SRC = os.path.join(CSRC, "oocdag_main.cpp")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -37,11 +40,11 @@ def _sources() -> list[str]:
 
 def _deps() -> list[str]:
     return _sources() + sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + sorted(
-        glob.glob(os.path.join(INCLUDE, "*.h")))
+        glob.glob(os.path.join(INCLUDE, "*.h"))) + [CLI_SRC]
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(p) <= t for p in _deps() + [__file__])
@@ -76,6 +79,14 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx:
+        cmd = [cxx, "-O2", "-std=c++17", "-I" + INCLUDE, CLI_SRC, "-L" + BUILD, "-loocdag_gb300",
+               "-Wl,-rpath,$ORIGIN", "-o", CLI + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

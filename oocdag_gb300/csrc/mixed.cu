@@ -144,15 +144,18 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
 
 // ---------------------------------------------------------------------------------
 // Column solve of a reduced-precision factor, in place:  P (m x LN, FP32, ld ldp) :=
-// P E^T with E = L_jj^{-1} (LN x LN, FP32, lower, exact zeros above the diagonal, ld
-// lde).  This is the dtrsm task (oocquark.cpp:130) as a product with the kept inverse.  One CTA per
+// P X^T with X = L_jj^{-1} (LN x LN, FP32, lower, exact zeros above the diagonal), given
+// row-major in Xr (ld ldxr).  This is the dtrsm task (oocquark.cpp:130) as a product with
+// the kept inverse.  One CTA per
 // 128-row block walks the 128-column blocks from the last to the first: output block cb
 // needs P's columns k < 128 (cb + 1) only, which no block written before it touches.
 // ---------------------------------------------------------------------------------
-__global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P, i64 ldp, const float* __restrict__ E,
-                                                          i64 lde, int m, int LN, const int* status) {
+constexpr int FBP = FB + 4;  // B slab row stride: float4-aligned, few bank conflicts on the transposed store
+
+__global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P, i64 ldp, const float* __restrict__ Xr,
+                                                          i64 ldxr, int m, int LN, const int* status) {
   if (status && *(volatile const int*)status) return;
-  __shared__ __align__(16) float smem[4 * FK * FB];  // A, B slabs (x2), reused as output stage
+  __shared__ __align__(16) float smem[2 * FK * FB + 2 * FK * FBP];  // A, B slabs (x2), reused as output stage
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int warp = tid >> 5, lane = tid & 31;
@@ -175,28 +178,30 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
         const int kc = idx / FB, x = idx % FB;
         const int gk = k0 + kc;
         ra[u] = (r0 + x < m && gk < kend) ? P[(r0 + x) + (i64)gk * ldp] : 0.f;
-        rb[u] = (c0 + x < LN && gk < kend) ? E[(c0 + x) + (i64)gk * lde] : 0.f;  // (E^T)(gk, c) = E(c, gk)
+        const int xb = idx / FK, kb2 = idx % FK;  // B: consecutive threads read consecutive k of X's row c
+        rb[u] = (c0 + xb < LN && k0 + kb2 < kend) ? Xr[(i64)(c0 + xb) * ldxr + k0 + kb2] : 0.f;  // (X^T)(k, c)
       }
     };
     fetch(0);
     for (int s = 0; s < nslab; s++) {
-      float* as_w = smem + (s & 1) * FK * FB;  // A slab; the B slab follows 2 FK FB later
+      float* as_w = smem + (s & 1) * FK * FB;
+      float* bs_w = smem + 2 * FK * FB + (s & 1) * FK * FBP;
 #pragma unroll
       for (int u = 0; u < PER; u++) {
         const int idx = tid + u * FTHR;
         as_w[idx] = ra[u];
-        as_w[2 * FK * FB + idx] = rb[u];
+        bs_w[(idx % FK) * FBP + idx / FK] = rb[u];
       }
       __syncthreads();
       if (s + 1 < nslab) fetch((s + 1) * FK);
       const float* as = as_w;
-      const float* bs = as_w + 2 * FK * FB;
+      const float* bs = bs_w;
 #pragma unroll
       for (int k = 0; k < FK; k++) {
         const float4 a0 = *reinterpret_cast<const float4*>(as + k * FB + ty * 4);
         const float4 a1 = *reinterpret_cast<const float4*>(as + k * FB + 64 + ty * 4);
-        const float4 b0 = *reinterpret_cast<const float4*>(bs + k * FB + tx * 4);
-        const float4 b1 = *reinterpret_cast<const float4*>(bs + k * FB + 64 + tx * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(bs + k * FBP + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(bs + k * FBP + 64 + tx * 4);
         const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
@@ -240,8 +245,8 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
 // ---------------------------------------------------------------------------------
 // Diagonal tile of a reduced-precision factor, fused in one CTA and in FP32:
 //   L_jj = chol(D) (the dpotrf task, oocquark.cpp:87/393), X = L_jj^{-1},
-// in place in the FP32 working matrix: D's lower triangle := L_jj, E := X (lower, zeros
-// above, ld lde), Dinv := X^T (upper, zeros below, ld lde).
+// in place in the FP32 working matrix: D's lower triangle := L_jj, Dinv := X^T (upper,
+// zeros below, ld lde), Xr := X row-major (ld LN; the column solve reads it).
 // Both phases are left-looking over 32-wide blocks, so every element is computed in
 // registers from finished data (D itself and Xr, a row-major FP32 scratch copy of X with
 // ld LN, both L2-resident) and written once:
@@ -253,7 +258,9 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
 // A non-positive pivot writes info = col0 + j + 1 to the status word and stops.
 // ---------------------------------------------------------------------------------
 constexpr int DG_THREADS = 512, DG_B = 32, DG_LD = 33, DG_MAX = 512;
-constexpr size_t DG_SMEM = (size_t)(DG_MAX * DG_B + DG_MAX * DG_LD + 2 * DG_B * DG_LD + DG_B) * sizeof(float);
+constexpr int DG_WARPS = DG_THREADS / 32;
+constexpr size_t DG_SMEM =
+    (size_t)(DG_MAX * DG_B + DG_MAX * DG_LD + DG_WARPS * 32 * DG_LD + 2 * DG_B * DG_LD + DG_B) * sizeof(float);
 
 // acc[c] -= sum_{q in [q_lo, q_hi)} v(q) * S[q * 32 + c], v(q) = src[q * stride] (L2), with
 // q_lo rounded down to 8 and v masked below q_lo; loads run one group of 8 ahead.
@@ -293,6 +300,68 @@ __device__ __forceinline__ void dg_dot32(float acc[DG_B], const float* __restric
   }
 }
 
+// acc[c] += sum over q in [qa, qb) of v(q) S[q * 32 + c], v(q) = src[q * stride] for
+// q >= qmask, else 0; qa is a multiple of 8 and the same for the whole warp.
+__device__ __forceinline__ void dg_dot_range(float acc[DG_B], const float* src, i64 stride, int qa, int qb,
+                                             int qmask, const float* __restrict__ S) {
+  if (qa >= qb) return;
+  float nx[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    const int q = qa + u;
+    nx[u] = (q >= qmask && q < qb) ? src[q * stride] : 0.f;
+  }
+  for (int q0 = qa; q0 < qb; q0 += 8) {
+    float x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) x[u] = nx[u];
+    if (q0 + 8 < qb) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int q = q0 + 8 + u;
+        nx[u] = (q >= qmask && q < qb) ? src[q * stride] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const float4* b4 = reinterpret_cast<const float4*>(S + (q0 + u) * DG_B);
+#pragma unroll
+      for (int v = 0; v < DG_B / 4; v++) {
+        const float4 bb = b4[v];
+        acc[4 * v + 0] = fmaf(x[u], bb.x, acc[4 * v + 0]);
+        acc[4 * v + 1] = fmaf(x[u], bb.y, acc[4 * v + 1]);
+        acc[4 * v + 2] = fmaf(x[u], bb.z, acc[4 * v + 2]);
+        acc[4 * v + 3] = fmaf(x[u], bb.w, acc[4 * v + 3]);
+      }
+    }
+  }
+}
+
+// Splits `njobs` reductions of len[j] 32-wide steps over the CTA's warps: every job gets
+// one chunk, the rest go one at a time to the job with the longest chunk (ties to the
+// lower job).  For each warp w: its job (-1: none), its chunk's step range [a, b) and the
+// number of chunks of its job (the chunks of a job are consecutive warps).
+__device__ void dg_plan_all(const int* len, int njobs, int* job, int* qa, int* qb, int* nch) {
+  int ch[DG_WARPS];
+  for (int j = 0; j < DG_WARPS; j++) ch[j] = (j < njobs) ? 1 : 0;
+  for (int extra = DG_WARPS - njobs; extra > 0; extra--) {
+    int best = -1;
+    for (int j = 0; j < njobs; j++)
+      if (len[j] > ch[j] && (best < 0 || len[j] * ch[best] > len[best] * ch[j])) best = j;
+    if (best < 0) break;
+    ch[best]++;
+  }
+  int w = 0;
+  for (int j = 0; j < njobs; j++)
+    for (int c = 0; c < ch[j]; c++, w++) {
+      job[w] = j;
+      nch[w] = ch[j];
+      qa[w] = (len[j] * c) / ch[j];
+      qb[w] = (len[j] * (c + 1)) / ch[j];
+    }
+  for (; w < DG_WARPS; w++) { job[w] = -1; nch[w] = 0; qa[w] = 1; qb[w] = 0; }
+}
+
 // S[q * 32 + c] = Lw(r0 + c, q) for q < nq, c < cb (0 for c >= cb): every load of the
 // thread is issued before the first store (a loop with one load per iteration would
 // wait an L2 round trip per element).
@@ -313,62 +382,88 @@ __device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* Lw,
 }
 
 __global__ void __launch_bounds__(DG_THREADS, 1)
-    k_diag_f32(float* D, i64 ldd, int LN, i64 col0, float* __restrict__ Dinv, float* __restrict__ E, i64 lde,
-               float* __restrict__ Xr, int* status) {
+    k_diag_f32(float* D, i64 ldd, int LN, i64 col0, float* __restrict__ Dinv, i64 lde, float* __restrict__ Xr,
+               int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(16) float dsm[];
   float* S = dsm;                      // staged rows, q-major: S[q * 32 + r]
   float* Cs = S + DG_MAX * DG_B;       // phase 1: the block column being finished, Cs[t * DG_LD + c]
-  float* Dk = Cs + DG_MAX * DG_LD;     // L(K, K), Dk[r * DG_LD + c]
+  float* Ps = Cs + DG_MAX * DG_LD;     // per-warp partial sums, Ps[(w * 32 + lane) * DG_LD + c]
+  float* Dk = Ps + DG_WARPS * 32 * DG_LD;  // L(K, K), Dk[r * DG_LD + c]
   float* Li = Dk + DG_B * DG_LD;       // phase 2: L_II^{-1}, Li[r * DG_LD + c]
   float* dinv = Li + DG_B * DG_LD;     // 1 / L(k + c, k + c)
   __shared__ int s_fail;
+  __shared__ int s_job[DG_WARPS], s_qa[DG_WARPS], s_qb[DG_WARPS], s_nch[DG_WARPS];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   float* Lw = D;  // L overwrites A in place
   const i64 ldw = ldd;
   const i64 ldx = LN;  // Xr
   if (t == 0) s_fail = 0;
   __syncthreads();
-  // ---- phase 1: L = chol(D), block columns left to right
+  // ---- phase 1: L = chol(D), block columns left to right.  Block column K: the row tiles
+  // below k0 are the jobs, each a reduction over the K earlier block columns, split across
+  // the warps; the chunks' partial sums are added in order by the job's first warp.
   for (int k0 = 0; k0 < LN; k0 += DG_B) {
     const int kb = min(DG_B, LN - k0), mK = LN - k0;
+    const int K = k0 / DG_B, njobs = (mK + DG_B - 1) / DG_B;
+    if (t == 0) {
+      int len[DG_WARPS];
+      for (int j = 0; j < DG_WARPS; j++) len[j] = K;
+      dg_plan_all(len, njobs, s_job, s_qa, s_qb, s_nch);
+    }
     dg_stage(S, Lw, ldw, k0, k0, kb);
     __syncthreads();
-    if (t < mK) {
-      const int i = k0 + t;
+    const int job = s_job[warp], qa = s_qa[warp], qb = s_qb[warp], nch = s_nch[warp];
+    if (job >= 0) {
+      const int rr = job * DG_B + lane;  // row within the block column
       float acc[DG_B];
 #pragma unroll
-      for (int c = 0; c < DG_B; c++) acc[c] = (c < kb && c <= t) ? Lw[i + (i64)(k0 + c) * ldw] : 0.f;
-      dg_dot32(acc, Lw + i, ldw, 0, k0, S, -1.f);
+      for (int c = 0; c < DG_B; c++) acc[c] = 0.f;
+      if (rr < mK) dg_dot_range(acc, Lw + k0 + rr, ldw, qa * DG_B, qb * DG_B, 0, S);
 #pragma unroll
-      for (int c = 0; c < DG_B; c++) Cs[t * DG_LD + c] = acc[c];
+      for (int c = 0; c < DG_B; c++) Ps[(warp * 32 + lane) * DG_LD + c] = acc[c];
+    }
+    __syncthreads();
+    if (job >= 0 && qa == 0) {  // C = A - sum of the chunks, in chunk order
+      const int rr = job * DG_B + lane;
+      if (rr < mK) {
+        const int i = k0 + rr;
+        float cv[DG_B];
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) cv[c] = (c < kb && c <= rr) ? Lw[i + (i64)(k0 + c) * ldw] : 0.f;
+        for (int w2 = warp; w2 < warp + nch; w2++)
+#pragma unroll
+          for (int c = 0; c < DG_B; c++) cv[c] -= Ps[(w2 * 32 + lane) * DG_LD + c];
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) Cs[rr * DG_LD + c] = cv[c];
+      }
     }
     __syncthreads();
     if (warp == 0) {
       // 32 x 32 Cholesky in registers: lane r holds row r; column j travels by shuffles.
+      // Straight-line code (a non-positive pivot is recorded and replaced by 1 so the
+      // remaining steps stay finite; the first one is reported).
       float a[DG_B];
 #pragma unroll
-      for (int c = 0; c < DG_B; c++) a[c] = (lane < kb && c <= lane) ? Cs[lane * DG_LD + c] : 0.f;
-      bool bad = false;
+      for (int c = 0; c < DG_B; c++) a[c] = (lane < kb && c <= lane) ? Cs[lane * DG_LD + c] : ((c == lane) ? 1.f : 0.f);
+      int first_bad = DG_B;
 #pragma unroll
       for (int j = 0; j < DG_B; j++) {
-        if (j < kb && !bad) {
-          const float d = __shfl_sync(0xffffffffu, a[j], j);
-          if (!(d > 0.f)) {
-            bad = true;
-            if (lane == 0) { s_fail = 1; atomicCAS(status, 0, (int)(col0 + k0 + j + 1)); }
-          } else {
-            const float sq = sqrtf(d), inv = 1.f / sq;
-            if (lane == j) { a[j] = sq; dinv[j] = inv; }
-            if (lane > j) a[j] *= inv;
+        float d = __shfl_sync(0xffffffffu, a[j], j);
+        if (!(d > 0.f)) {
+          first_bad = min(first_bad, j);
+          d = 1.f;
+        }
+        const float inv = rsqrtf(d);
+        if (lane == j) { a[j] = d * inv; dinv[j] = inv; }
+        if (lane > j) a[j] *= inv;
 #pragma unroll
-            for (int c = j + 1; c < DG_B; c++) {
-              const float lcj = __shfl_sync(0xffffffffu, a[j], c);
-              if (lane >= c) a[c] = fmaf(-a[j], lcj, a[c]);
-            }
-          }
+        for (int c = j + 1; c < DG_B; c++) {
+          const float lcj = __shfl_sync(0xffffffffu, a[j], c);
+          if (lane >= c) a[c] = fmaf(-a[j], lcj, a[c]);
         }
       }
+      if (first_bad < kb && lane == 0) { s_fail = 1; atomicCAS(status, 0, (int)(col0 + k0 + first_bad + 1)); }
 #pragma unroll
       for (int c = 0; c < DG_B; c++) Dk[lane * DG_LD + c] = (c <= lane) ? a[c] : 0.f;
     }
@@ -398,16 +493,23 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     __syncthreads();
   }
   if (s_fail) return;
-  // ---- phase 2: X = L^{-1}, block rows top to bottom
+  // ---- phase 2: X = L^{-1}, block rows top to bottom.  Block row I: the column tiles jt < I
+  // are the jobs, each a reduction over the block rows jt .. I-1, split across the warps.
   for (int i0 = 0; i0 < LN; i0 += DG_B) {
-    const int ib = min(DG_B, LN - i0);
+    const int ib = min(DG_B, LN - i0), I = i0 / DG_B;
+    if (t == 0) {
+      int len[DG_WARPS];
+      for (int j = 0; j < DG_WARPS; j++) len[j] = I - j;
+      dg_plan_all(len, I < DG_WARPS ? I : DG_WARPS, s_job, s_qa, s_qb, s_nch);
+    }
     dg_stage(S, Lw, ldw, i0, i0, ib);
     for (int idx = t; idx < DG_B * DG_B; idx += DG_THREADS) {
       const int r = idx >> 5, c = idx & 31;
       Dk[r * DG_LD + c] = (r < ib && c <= r) ? Lw[(i0 + r) + (i0 + c) * ldw] : 0.f;
     }
     __syncthreads();
-    if (warp == 0) {  // L_II^{-1}: lane c solves L_II x = e_c
+    const int job = s_job[warp], qa = s_qa[warp], qb = s_qb[warp], nch = s_nch[warp];
+    if (warp == DG_WARPS - 1) {  // L_II^{-1}: lane c solves L_II x = e_c (concurrently with the chunks)
       float x[DG_B];
 #pragma unroll
       for (int r = 0; r < DG_B; r++) {
@@ -419,13 +521,25 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
 #pragma unroll
       for (int r = 0; r < DG_B; r++) Li[r * DG_LD + lane] = x[r];
     }
-    __syncthreads();
-    if (t < i0) {
-      const int j = t;
+    if (job >= 0) {
+      const int j = job * DG_B + lane;  // column of X
       float acc[DG_B];
 #pragma unroll
       for (int r = 0; r < DG_B; r++) acc[r] = 0.f;
-      dg_dot32(acc, Xr + j, ldx, j, i0, S, 1.f);  // acc[r] = sum_q L(i0 + r, q) X(q, j)
+      // acc[r] = sum_q L(i0 + r, q) X(q, j) over the chunk's block rows jt + qa .. jt + qb - 1
+      dg_dot_range(acc, Xr + j, ldx, (job + qa) * DG_B, (job + qb) * DG_B, j, S);
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) Ps[(warp * 32 + lane) * DG_LD + r] = acc[r];
+    }
+    __syncthreads();
+    if (job >= 0 && qa == 0) {
+      const int j = job * DG_B + lane;
+      float acc[DG_B];
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) acc[r] = 0.f;
+      for (int w2 = warp; w2 < warp + nch; w2++)
+#pragma unroll
+        for (int r = 0; r < DG_B; r++) acc[r] += Ps[(w2 * 32 + lane) * DG_LD + r];
       float y[DG_B];
 #pragma unroll
       for (int r = 0; r < DG_B; r++) {
@@ -438,22 +552,28 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
       for (int r = 0; r < DG_B; r++)
         if (r < ib) {
           Xr[(i0 + r) * ldx + j] = y[r];
-          E[(i0 + r) + (i64)j * lde] = y[r];
           Dinv[j + (i64)(i0 + r) * lde] = y[r];
         }
-    } else if (t < LN) {
+    }
+    if (t >= i0 && t < LN) {
       const int c = t - i0;  // diagonal block column (c < ib) or right of it (zeros)
 #pragma unroll
       for (int r = 0; r < DG_B; r++)
         if (r < ib) {
           const float y = (c < ib && r >= c) ? Li[r * DG_LD + c] : 0.f;
-          if (c < ib) Xr[(i0 + r) * ldx + t] = y;
-          E[(i0 + r) + (i64)t * lde] = y;
+          Xr[(i0 + r) * ldx + t] = y;
           Dinv[t + (i64)(i0 + r) * lde] = y;
         }
     }
     __syncthreads();
   }
+}
+
+// FP32 column panel (m x K, ld ldx) -> copy with ld ldy.
+__global__ void k_copy_f32(const float* __restrict__ X, i64 ldx, float* __restrict__ Y, i64 ldy, int m, int K) {
+  const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  for (int k = blockIdx.y; k < K; k += gridDim.y) Y[r + k * ldy] = X[r + k * ldx];
 }
 
 // FP64 column panel (m x K, ld ldx) -> FP32 copy (ld ldy).
@@ -884,7 +1004,21 @@ int syrk_f32(int prec, const float* X, i64 ldx, float* C, i64 ldc, int m, int K,
     if (bj_lo >= hi) return OOC_OK;
     const i64 nblk = ooc_lower_blocks_before(hi, T) - ooc_lower_blocks_before(bj_lo, T);
     if (nblk > 0x7fffffff) return OOC_ERR_INTERNAL;
-    k_syrk_f32<float><<<(unsigned)nblk, FTHR, 0, s>>>(X, ldx, C, ldc, m, K, (int)T, bj_lo, status);
+    // k_syrk_f32 stages X with 16-byte copies: a panel whose base or leading dimension is
+    // not 16-byte compatible is first copied to an aligned buffer (once per panel).
+    const float* Xs = X;
+    i64 lds = ldx;
+    if ((reinterpret_cast<uintptr_t>(X) % 16) != 0 || (ldx % 4) != 0) {
+      lds = ((i64)m + 3) / 4 * 4;
+      if (prepare) {
+        int rc = work.ensure((size_t)lds * K * sizeof(float));
+        if (rc) return rc;
+        k_copy_f32<<<dim3((unsigned)((m + 255) / 256), (unsigned)std::min(K, 1024)), 256, 0, s>>>(X, ldx, (float*)work.p,
+                                                                                              lds, m, K);
+      }
+      Xs = (const float*)work.p;
+    }
+    k_syrk_f32<float><<<(unsigned)nblk, FTHR, 0, s>>>(Xs, lds, C, ldc, m, K, (int)T, bj_lo, status);
     OOC_CUDA_TRY(cudaGetLastError());
     return OOC_OK;
   }
@@ -1019,7 +1153,9 @@ struct ooc_factor {
   // diagonal inverses; the FP64 members stay null.
   double* L = nullptr;     // n x n, ld n (owned); lower = factor
   double* Dinv = nullptr;  // bb tiles of nb x nb: L_JJ^{-T}
-  float* Lf = nullptr;     // n x n FP32, ld n
+  float* Lf = nullptr;     // n x n FP32, ld `ld`
+  i64 ld = 0;              // leading dimension of Lf (n for a factor object)
+  bool owns_Lf = true;     // false when Lf is a caller's matrix (ooc_spotrf_L)
   float* Dinvf = nullptr;
   double* tmp = nullptr;   // nb x 16
   float* tmpf = nullptr;
@@ -1029,7 +1165,7 @@ struct ooc_factor {
   ~ooc_factor() {
     if (L) cudaFree(L);
     if (Dinv) cudaFree(Dinv);
-    if (Lf) cudaFree(Lf);
+    if (Lf && owns_Lf) cudaFree(Lf);
     if (Dinvf) cudaFree(Dinvf);
     if (tmp) cudaFree(tmp);
     if (tmpf) cudaFree(tmpf);
@@ -1163,20 +1299,19 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
 //   s0: the column solve (FP32 product with the inverse, in place, every SM), then the
 //       trailing update in `prec` -- the next panel's block columns first (an event lets
 //       s1 start on its diagonal tile), then the rest.
-constexpr int kChainSMs = 8;
+constexpr int kChainSMs = 1;  // the diagonal kernel is one CTA
 
 int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
   const int bb = (int)((n + nb - 1) / nb);
   float* A = F->Lf;
-  const i64 lda = n;
+  const i64 lda = F->ld;
   const i64 tile = (i64)nb * nb;
   if (nb > DG_MAX) return OOC_ERR_UNSUPPORTED;
-  int rc = F->scratch.ensure((size_t)2 * tile * sizeof(float));
+  int rc = F->scratch.ensure((size_t)tile * sizeof(float));
   if (rc) return rc;
-  float* E = (float*)F->scratch.p;  // L_jj^{-1} (lower, ld nb)
-  float* Xr = E + tile;             // row-major copy for the diagonal kernel
+  float* Xr = (float*)F->scratch.p;  // L_jj^{-1}, row-major (ld LN), from the diagonal kernel
   const bool split = (nb % 128 == 0);
   OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
   cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: diagonal tile done (s1 -> s0)
@@ -1193,7 +1328,7 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     float* Djj = A + J0 + J0 * lda;
     OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
     if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, E, nb, Xr, F->status);
+    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, nb, Xr, F->status);
     OOC_CUDA_TRY(cudaGetLastError());
     if (prof->on) prof->mark(s1);
     OOC_CUDA_TRY(cudaEventRecord(evP, s1));
@@ -1202,7 +1337,7 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     if (m > 0) {
       float* Pn = Djj + LN;
       if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
-      k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, E, nb, (int)m, LN, F->status);
+      k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN, F->status);
       OOC_CUDA_TRY(cudaGetLastError());
       if (prof->on) {
         prof->mark(s0);
@@ -1258,6 +1393,7 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   ooc_factor* F = new ooc_factor();
   F->device = ooc_device(h);
   F->n = n;
+  F->ld = n;
   F->nb = nb;
   F->prec = prec;
   int rc = alloc_factor(F, n, nb, reduced);
@@ -1679,4 +1815,95 @@ extern "C" int ooc_dsyrk_ln(ooc_handle* h, int prec, int n, int k, const double*
   cudaFree(status);
   if (rc) return rc;
   return st == 0 ? OOC_OK : OOC_ERR_TIMEOUT;
+}
+
+// ---------------------------------------------------------------------------------
+// FP32 Cholesky of a caller's matrix, in place (the reference has no FP32 entry): the
+// reduced-precision factor pipeline with FP32 trailing updates (k_syrk_f32), on the
+// matrix itself (device) or on a device copy of it (host, when it fits in dev_budget).
+// ---------------------------------------------------------------------------------
+extern "C" int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int nb, size_t dev_budget, int* info,
+                            ooc_stats* stats) {
+  if (!h) return -1;
+  if (!A && n > 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max<int64_t>(1, n)) return -4;
+  if (nb <= 0 || nb > DG_MAX) return -5;
+  if (!info) return -7;
+  *info = 0;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (n == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  cudaPointerAttributes pa{};
+  const bool on_device = cudaPointerGetAttributes(&pa, A) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  ooc_factor F;
+  F.device = ooc_device(h);
+  F.n = n;
+  F.nb = nb;
+  F.prec = OOC_PREC_FP32;
+  F.owns_Lf = on_device ? false : true;
+  const int bb = (int)((n + nb - 1) / nb);
+  if (on_device) {
+    F.Lf = A;
+    F.ld = lda;
+  } else {
+    const size_t bytes = (size_t)n * n * sizeof(float);
+    size_t budget = dev_budget;
+    if (budget == 0) {
+      size_t fr = 0, tot = 0;
+      cudaMemGetInfo(&fr, &tot);
+      budget = fr / 4 * 3;
+    }
+    if (bytes > budget) {
+      ooc_set_last_message("ooc_spotrf_L: a host matrix is factored on a device copy, which exceeds the budget");
+      return OOC_ERR_BUDGET;
+    }
+    if (cudaMalloc(&F.Lf, bytes) != cudaSuccess) { cudaGetLastError(); F.Lf = nullptr; return OOC_ERR_NOMEM; }
+    F.ld = n;
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(F.Lf, n * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,
+                                   cudaMemcpyHostToDevice, s));
+  }
+  if (cudaMalloc(&F.Dinvf, (size_t)bb * nb * nb * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&F.status, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return OOC_ERR_NOMEM;
+  }
+  OOC_CUDA_TRY(cudaMemsetAsync(F.status, 0, sizeof(int), s));
+  cudaEvent_t e0, e1;
+  OOC_CUDA_TRY(cudaEventCreate(&e0));
+  OOC_CUDA_TRY(cudaEventCreate(&e1));
+  OOC_CUDA_TRY(cudaEventRecord(e0, s));
+  void* s1p = nullptr;
+  ooc_get_stream(h, 1, &s1p);
+  MixedProf prof;
+  int64_t launches = 0;
+  int rc = factor_f32(&F, OOC_PREC_FP32, s, (cudaStream_t)s1p, &launches, &prof);
+  if (!rc) rc = cudaEventRecord(e1, s) == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+  int st = 0;
+  if (!rc) rc = read_int(F.status, &st, s);
+  if (!rc && !on_device)
+    rc = cudaMemcpy2D(A, lda * sizeof(float), F.Lf, n * sizeof(float), n * sizeof(float), n, cudaMemcpyDeviceToHost) ==
+                 cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { ooc_set_last_error(e, "ooc_spotrf_L", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
+  }
+  float ms = 0;
+  if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  *info = st;
+  if (stats) {
+    stats->seconds = ms * 1e-3;
+    stats->flops = (double)n * n * n / 3.0;
+    stats->npanels = 1;
+    stats->info = st;
+    stats->kernel_launches = launches;
+    stats->h2d_bytes = on_device ? 0.0 : (double)n * n * 4;
+    stats->d2h_bytes = on_device ? 0.0 : (double)n * n * 4;
+  }
+  return OOC_OK;
 }

@@ -45,6 +45,8 @@ constexpr int TMEM_COLS = NACC * TB;
 constexpr int EPI_WARPS = 16;                     // four per TMEM lane quadrant (32 columns each)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;      // producer warp, MMA warp, epilogue
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+// barriers, TMEM address and abort flag must end before the two counters at offset 128
+static_assert((2 * STAGES + 2 * NACC + 1) * 8 + 8 <= 128, "control block overflow");
 constexpr int STRIP = 16;                         // block columns per scheduling strip
 constexpr long long WAIT_LIMIT = 1LL << 22;       // polls before a wait is declared stuck
 constexpr int ERR_TIMEOUT_CODE = -1000003;        // status value written on a stuck wait
@@ -264,8 +266,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         int bi, bj;
         strip_block_decode(t, T, bj_lo, bj_hi, &bi, &bj);
         const bool diag = (bi == bj);
-        const int acc = tl & 1;
-        if (!mbar_wait(&tempty[acc], (uint32_t)(((tl >> 1) & 1) ^ 1), abort_flag)) { ok = false; break; }
+        const int acc = tl % NACC;
+        if (!mbar_wait(&tempty[acc], (uint32_t)(((tl / NACC) & 1) ^ 1), abort_flag)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
         const uint32_t dt = tmem + (uint32_t)(acc * TB);
         for (int kc = 0; kc < nk; kc++, c++) {
@@ -315,8 +317,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
     }
     for (; t < nblk; t += gridDim.x, tl++) {
-      const int acc = tl & 1;
-      const bool got = mbar_wait(&tfull[acc], (uint32_t)((tl >> 1) & 1), abort_flag);
+      const int acc = tl % NACC;
+      const bool got = mbar_wait(&tfull[acc], (uint32_t)((tl / NACC) & 1), abort_flag);
       if (!__all_sync(0xffffffffu, got)) {
         if (lane == 0) *abort_flag = 1;
         break;
