@@ -45,6 +45,7 @@ METRIC = "Cholesky TFLOP/s (n^3/3 flops), mixed vs FP64 at backward err<=1e-14; 
 # 44.02 GFLOP; profiles/k_panel_update_fp64_n8192.md).  The kernel's traffic is the
 # operand and C tiles, which scale with the flops of a launch at fixed nb.
 UPDATE_DRAM_BYTES_PER_FLOP = 348.1e6 / 44.02e9
+UPDATE_TRAFFIC_RATIO = 988.1 / 976.0  # tcgen05 update: ncu DRAM bytes / algorithmic bytes
 
 
 def parse():
@@ -539,16 +540,28 @@ def run_mixed(args):
         Bd = torch.empty((nrhs, n), dtype=torch.float64, device="cuda")
         Xd = torch.empty_like(Bd)
 
-        def e2e_step():
+        phase = {"h2d_ms": 0.0, "factor_ms": 0.0, "refine_ms": 0.0, "close_ms": 0.0, "d2h_ms": 0.0}
+
+        def e2e_step(record=False):
+            t0 = time.perf_counter()
             with torch.cuda.stream(comp):
                 Ad.copy_(Ah, non_blocking=True)
                 Bd.copy_(Bh, non_blocking=True)
+            comp.synchronize()
+            t1 = time.perf_counter()
             F = h.factor(Ad, n, n, nb, args.prec)
+            t2 = time.perf_counter()
             F.refine(Ad, n, Bd, n, Xd, n, nrhs, 1e-14, 30)
+            t3 = time.perf_counter()
             F.close()
+            t4 = time.perf_counter()
             with torch.cuda.stream(comp):
                 Xh.copy_(Xd, non_blocking=True)
             comp.synchronize()
+            t5 = time.perf_counter()
+            if record:
+                for k, v in zip(phase, (t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4)):
+                    phase[k] += v * 1e3 / args.steps
 
         for _ in range(args.warmup):
             e2e_step()
@@ -557,12 +570,13 @@ def run_mixed(args):
         s1 = torch.cuda.Event(enable_timing=True)
         s0.record(comp)
         for _ in range(args.steps):
-            e2e_step()
+            e2e_step(record=True)
         s1.record(comp)
         torch.cuda.synchronize()
         e_ms = allreduce_max(s0.elapsed_time(s1) / args.steps, world)
         e2e = {"value": flops * world / (e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e_ms,
-               "h2d_bytes_per_step": int(n * n * 8 + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8)}
+               "h2d_bytes_per_step": int(n * n * 8 + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8),
+               "phases_ms_host_clock": {k: round(v, 2) for k, v in phase.items()}}
         del Ah, Bh, Xh, Ad, Bd, Xd
 
     # ---- roofline of the dominant kernel ------------------------------------------------
@@ -570,11 +584,13 @@ def run_mixed(args):
     # m (m+1) K useful flops, three BF16 tensor products of each (hi*hi, hi*lo, lo*hi); bytes:
     # the FP32 lower triangle read and written (8 B per element), the FP32 panel read by the
     # split (4 B per element) and the two BF16 planes written and read once (8 B per element).
-    upd_bytes = 0.0
+    upd_bytes = kern_bytes = 0.0
     for j in range(n // nb - 1):
         m = n - (j + 1) * nb
         upd_bytes += m * (m + 1) / 2 * 8 + m * nb * (4 + 8)
+        kern_bytes += m * (m + 1) / 2 * 8 + m * nb * 4  # what the tcgen05 kernel itself moves
     upd_bytes *= args.steps
+    kern_bytes *= args.steps
     share_upd = upd_ms / (ms_local * args.steps)
     share_fac = fac_ms / (ms_local * args.steps)
     bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
@@ -592,6 +608,12 @@ def run_mixed(args):
                                "seconds-long step)"}
     if upd_roof["achieved"] and upd_roof["peak"]:
         upd_roof["frac"] = upd_roof["achieved"] / upd_roof["peak"]
+    if args.prec == "bf16x3" and upd_launch:
+        # DRAM bytes per launch: the algorithmic kernel bytes scaled by the measured/algorithmic
+        # ratio of one ncu capture (bulk update at n=16384: 988.1 MB measured, 976 MB algorithmic)
+        upd_roof["traffic"] = UPDATE_TRAFFIC_RATIO * kern_bytes / upd_launch
+        upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk-update launch "
+                                      "(kernel_bench mixed --n 16384), scaled to this workload's launches")
     chain_flops = sum(2 * nb ** 3 / 3 + (n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_f32 (FP32 potrf + inverse of the 512x512 tile, one CTA) + "
                           "k_colsolve_f32 (FP32 column solve)",
@@ -601,7 +623,7 @@ def run_mixed(args):
                 "note": "segments on two streams overlap the update; share is their summed device time"}
     dominant, other = (upd_roof, fac_roof) if share_upd >= share_fac else (fac_roof, upd_roof)
     roofline = dict(dominant)
-    roofline["traffic"] = None
+    roofline.setdefault("traffic", None)
     roofline["next_kernel"] = other
 
     cpu = None

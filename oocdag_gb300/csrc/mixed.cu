@@ -146,73 +146,78 @@ __global__ void __launch_bounds__(FTHR) k_syrk_f32(const float* __restrict__ X, 
 // Column solve of a reduced-precision factor, in place:  P (m x LN, FP32, ld ldp) :=
 // P X^T with X = L_jj^{-1} (LN x LN, FP32, lower, exact zeros above the diagonal), given
 // row-major in Xr (ld ldxr).  This is the dtrsm task (oocquark.cpp:130) as a product with
-// the kept inverse.  One CTA per
-// 128-row block walks the 128-column blocks from the last to the first: output block cb
-// needs P's columns k < 128 (cb + 1) only, which no block written before it touches.
+// the kept inverse.  One CTA per 64-row block walks the 128-column blocks from the last to
+// the first: output block cb needs P's columns k < 128 (cb + 1) only, which no block
+// written before it touches.
 // ---------------------------------------------------------------------------------
-constexpr int FBP = FB + 4;  // B slab row stride: float4-aligned, few bank conflicts on the transposed store
+constexpr int CS_ROWS = 64;           // rows per CTA
+constexpr int CS_COLS = 128;          // output columns per pass
+constexpr int CS_BP = CS_COLS + 4;    // B slab row stride: float4-aligned, few bank conflicts on the transposed store
 
 __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P, i64 ldp, const float* __restrict__ Xr,
                                                           i64 ldxr, int m, int LN, const int* status) {
   if (status && *(volatile const int*)status) return;
-  __shared__ __align__(16) float smem[2 * FK * FB + 2 * FK * FBP];  // A, B slabs (x2), reused as output stage
+  __shared__ __align__(16) float smem[2 * FK * CS_ROWS + 2 * FK * CS_BP];  // A, B slabs (x2), then output stage
   const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
+  const int tx = tid & 15, ty = tid >> 4;  // 8 columns (tx*4.., 64+tx*4..) x 4 rows (ty*4..)
   const int warp = tid >> 5, lane = tid & 31;
-  const int r0 = blockIdx.x * FB;
-  constexpr int PER = FK * FB / FTHR;  // 8 staged elements per thread and operand
-  for (int cb = (LN - 1) / FB; cb >= 0; cb--) {
-    const int c0 = cb * FB;
-    const int kend = min(LN, c0 + FB);
+  const int r0 = blockIdx.x * CS_ROWS;
+  constexpr int PA = FK * CS_ROWS / FTHR;  // 4 A elements per thread and slab
+  constexpr int PB = FK * CS_COLS / FTHR;  // 8 B elements per thread and slab
+  for (int cb = (LN - 1) / CS_COLS; cb >= 0; cb--) {
+    const int c0 = cb * CS_COLS;
+    const int kend = min(LN, c0 + CS_COLS);
     const int nslab = (kend + FK - 1) / FK;
-    float acc[8][8];
+    float acc[4][8];
 #pragma unroll
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < 4; i++)
 #pragma unroll
       for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
-    float ra[PER], rb[PER];
+    float ra[PA], rb[PB];
     auto fetch = [&](int k0) {
 #pragma unroll
-      for (int u = 0; u < PER; u++) {
+      for (int u = 0; u < PA; u++) {
         const int idx = tid + u * FTHR;
-        const int kc = idx / FB, x = idx % FB;
+        const int kc = idx / CS_ROWS, x = idx % CS_ROWS;
         const int gk = k0 + kc;
         ra[u] = (r0 + x < m && gk < kend) ? P[(r0 + x) + (i64)gk * ldp] : 0.f;
-        const int xb = idx / FK, kb2 = idx % FK;  // B: consecutive threads read consecutive k of X's row c
+      }
+#pragma unroll
+      for (int u = 0; u < PB; u++) {
+        const int idx = tid + u * FTHR;
+        const int xb = idx / FK, kb2 = idx % FK;  // consecutive threads read consecutive k of X's row c
         rb[u] = (c0 + xb < LN && k0 + kb2 < kend) ? Xr[(i64)(c0 + xb) * ldxr + k0 + kb2] : 0.f;  // (X^T)(k, c)
       }
     };
     fetch(0);
     for (int s = 0; s < nslab; s++) {
-      float* as_w = smem + (s & 1) * FK * FB;
-      float* bs_w = smem + 2 * FK * FB + (s & 1) * FK * FBP;
+      float* as_w = smem + (s & 1) * FK * CS_ROWS;
+      float* bs_w = smem + 2 * FK * CS_ROWS + (s & 1) * FK * CS_BP;
 #pragma unroll
-      for (int u = 0; u < PER; u++) {
+      for (int u = 0; u < PA; u++) as_w[tid + u * FTHR] = ra[u];
+#pragma unroll
+      for (int u = 0; u < PB; u++) {
         const int idx = tid + u * FTHR;
-        as_w[idx] = ra[u];
-        bs_w[(idx % FK) * FBP + idx / FK] = rb[u];
+        bs_w[(idx % FK) * CS_BP + idx / FK] = rb[u];
       }
       __syncthreads();
       if (s + 1 < nslab) fetch((s + 1) * FK);
-      const float* as = as_w;
-      const float* bs = bs_w;
 #pragma unroll
       for (int k = 0; k < FK; k++) {
-        const float4 a0 = *reinterpret_cast<const float4*>(as + k * FB + ty * 4);
-        const float4 a1 = *reinterpret_cast<const float4*>(as + k * FB + 64 + ty * 4);
-        const float4 b0 = *reinterpret_cast<const float4*>(bs + k * FBP + tx * 4);
-        const float4 b1 = *reinterpret_cast<const float4*>(bs + k * FBP + 64 + tx * 4);
-        const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float4 a0 = *reinterpret_cast<const float4*>(as_w + k * CS_ROWS + ty * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(bs_w + k * CS_BP + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(bs_w + k * CS_BP + 64 + tx * 4);
+        const float a[4] = {a0.x, a0.y, a0.z, a0.w};
         const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-        for (int i = 0; i < 8; i++)
+        for (int i = 0; i < 4; i++)
 #pragma unroll
           for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
       }
     }
     __syncthreads();  // every read of P's columns < kend is done before any store below
-    // Store through shared memory 32 columns at a time (stride 129) so each warp writes
-    // whole column segments (coalesced).
+    // Store through shared memory 32 columns at a time (stride CS_ROWS + 1) so each warp
+    // writes whole column segments (coalesced).
     float* stage = smem;
 #pragma unroll
     for (int qtr = 0; qtr < 4; qtr++) {
@@ -220,11 +225,9 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
       const int lo_tx = (qtr & 1) * 8;
       if (tx >= lo_tx && tx < lo_tx + 8) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const int rr = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+        for (int i = 0; i < 4; i++)
 #pragma unroll
-          for (int j = 0; j < 4; j++) stage[((tx - lo_tx) * 4 + j) * 129 + rr] = acc[i][half * 4 + j];
-        }
+          for (int j = 0; j < 4; j++) stage[((tx - lo_tx) * 4 + j) * (CS_ROWS + 1) + ty * 4 + i] = acc[i][half * 4 + j];
       }
       __syncthreads();
 #pragma unroll
@@ -232,9 +235,9 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
         const int cc = warp * 4 + u;
         const int c = c0 + half * 64 + (qtr & 1) * 32 + cc;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < 2; q++) {
           const int rr = lane + 32 * q;
-          if (c < LN && r0 + rr < m) P[(r0 + rr) + (i64)c * ldp] = stage[cc * 129 + rr];
+          if (c < LN && r0 + rr < m) P[(r0 + rr) + (i64)c * ldp] = stage[cc * (CS_ROWS + 1) + rr];
         }
       }
       __syncthreads();
@@ -259,46 +262,11 @@ __global__ void __launch_bounds__(FTHR, 2) k_colsolve_f32(float* __restrict__ P,
 // ---------------------------------------------------------------------------------
 constexpr int DG_THREADS = 512, DG_B = 32, DG_LD = 33, DG_MAX = 512;
 constexpr int DG_WARPS = DG_THREADS / 32;
+constexpr int DG_STEPS = 2 * (DG_MAX / DG_B);  // phase 1 and phase 2 steps
 constexpr size_t DG_SMEM =
-    (size_t)(DG_MAX * DG_B + DG_MAX * DG_LD + DG_WARPS * 32 * DG_LD + 2 * DG_B * DG_LD + DG_B) * sizeof(float);
+    (size_t)(DG_MAX * DG_B + DG_MAX * DG_LD + DG_WARPS * 32 * DG_LD + 2 * DG_B * DG_LD + DG_B) * sizeof(float) +
+    (size_t)DG_STEPS * DG_WARPS * sizeof(int4);
 
-// acc[c] -= sum_{q in [q_lo, q_hi)} v(q) * S[q * 32 + c], v(q) = src[q * stride] (L2), with
-// q_lo rounded down to 8 and v masked below q_lo; loads run one group of 8 ahead.
-__device__ __forceinline__ void dg_dot32(float acc[DG_B], const float* __restrict__ src, i64 stride, int q_lo,
-                                         int q_hi, const float* __restrict__ S, float sign) {
-  const int q0s = q_lo & ~7;
-  if (q0s >= q_hi) return;
-  float nx[8];
-#pragma unroll
-  for (int u = 0; u < 8; u++) {
-    const int q = q0s + u;
-    nx[u] = (q >= q_lo && q < q_hi) ? src[q * stride] : 0.f;
-  }
-  for (int q0 = q0s; q0 < q_hi; q0 += 8) {
-    float x[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) x[u] = nx[u] * sign;
-    if (q0 + 8 < q_hi) {
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int q = q0 + 8 + u;
-        nx[u] = (q < q_hi) ? src[q * stride] : 0.f;
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const float4* b4 = reinterpret_cast<const float4*>(S + (q0 + u) * DG_B);
-#pragma unroll
-      for (int v = 0; v < DG_B / 4; v++) {
-        const float4 bb = b4[v];
-        acc[4 * v + 0] = fmaf(x[u], bb.x, acc[4 * v + 0]);
-        acc[4 * v + 1] = fmaf(x[u], bb.y, acc[4 * v + 1]);
-        acc[4 * v + 2] = fmaf(x[u], bb.z, acc[4 * v + 2]);
-        acc[4 * v + 3] = fmaf(x[u], bb.w, acc[4 * v + 3]);
-      }
-    }
-  }
-}
 
 // acc[c] += sum over q in [qa, qb) of v(q) S[q * 32 + c], v(q) = src[q * stride] for
 // q >= qmask, else 0; qa is a multiple of 8 and the same for the whole warp.
@@ -392,28 +360,42 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
   float* Dk = Ps + DG_WARPS * 32 * DG_LD;  // L(K, K), Dk[r * DG_LD + c]
   float* Li = Dk + DG_B * DG_LD;       // phase 2: L_II^{-1}, Li[r * DG_LD + c]
   float* dinv = Li + DG_B * DG_LD;     // 1 / L(k + c, k + c)
+  int4* plan = reinterpret_cast<int4*>(dinv + DG_B);  // [step][warp] = (job, qa, qb, nch)
   __shared__ int s_fail;
-  __shared__ int s_job[DG_WARPS], s_qa[DG_WARPS], s_qb[DG_WARPS], s_nch[DG_WARPS];
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   float* Lw = D;  // L overwrites A in place
   const i64 ldw = ldd;
   const i64 ldx = LN;  // Xr
   if (t == 0) s_fail = 0;
+  // Work plans of all steps, one thread per step (phase 1: block column K, jobs = row tiles
+  // of length K; phase 2: block row I, jobs = column tiles jt of length I - jt).
+  const int nsteps = (LN + DG_B - 1) / DG_B;
+  if (t < 2 * nsteps) {
+    int len[DG_WARPS], job[DG_WARPS], qa[DG_WARPS], qb[DG_WARPS], nch[DG_WARPS];
+    int njobs;
+    if (t < nsteps) {
+      const int K = t;
+      njobs = (LN - K * DG_B + DG_B - 1) / DG_B;
+      for (int j = 0; j < DG_WARPS; j++) len[j] = K;
+    } else {
+      const int I = t - nsteps;
+      njobs = I < DG_WARPS ? I : DG_WARPS;
+      for (int j = 0; j < DG_WARPS; j++) len[j] = I - j;
+    }
+    dg_plan_all(len, njobs, job, qa, qb, nch);
+    for (int w = 0; w < DG_WARPS; w++) plan[t * DG_WARPS + w] = make_int4(job[w], qa[w], qb[w], nch[w]);
+  }
   __syncthreads();
   // ---- phase 1: L = chol(D), block columns left to right.  Block column K: the row tiles
   // below k0 are the jobs, each a reduction over the K earlier block columns, split across
   // the warps; the chunks' partial sums are added in order by the job's first warp.
   for (int k0 = 0; k0 < LN; k0 += DG_B) {
     const int kb = min(DG_B, LN - k0), mK = LN - k0;
-    const int K = k0 / DG_B, njobs = (mK + DG_B - 1) / DG_B;
-    if (t == 0) {
-      int len[DG_WARPS];
-      for (int j = 0; j < DG_WARPS; j++) len[j] = K;
-      dg_plan_all(len, njobs, s_job, s_qa, s_qb, s_nch);
-    }
+    const int K = k0 / DG_B;
     dg_stage(S, Lw, ldw, k0, k0, kb);
     __syncthreads();
-    const int job = s_job[warp], qa = s_qa[warp], qb = s_qb[warp], nch = s_nch[warp];
+    const int4 pw = plan[K * DG_WARPS + warp];
+    const int job = pw.x, qa = pw.y, qb = pw.z, nch = pw.w;
     if (job >= 0) {
       const int rr = job * DG_B + lane;  // row within the block column
       float acc[DG_B];
@@ -440,28 +422,33 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
     }
     __syncthreads();
     if (warp == 0) {
-      // 32 x 32 Cholesky in registers: lane r holds row r; column j travels by shuffles.
-      // Straight-line code (a non-positive pivot is recorded and replaced by 1 so the
-      // remaining steps stay finite; the first one is reported).
+      // 32 x 32 Cholesky in registers: lane r holds row r.  Column j is published through
+      // shared memory (one store, then independent broadcast loads), not shuffles whose
+      // latency each update would wait for.  Straight-line code: a non-positive pivot is
+      // recorded and replaced by 1 so the remaining steps stay finite; the first is reported.
       float a[DG_B];
+      float* colb = Li;  // free during phase 1
 #pragma unroll
       for (int c = 0; c < DG_B; c++) a[c] = (lane < kb && c <= lane) ? Cs[lane * DG_LD + c] : ((c == lane) ? 1.f : 0.f);
       int first_bad = DG_B;
 #pragma unroll
       for (int j = 0; j < DG_B; j++) {
-        float d = __shfl_sync(0xffffffffu, a[j], j);
+        colb[lane] = a[j];
+        __syncwarp();
+        float d = colb[j];
         if (!(d > 0.f)) {
           first_bad = min(first_bad, j);
           d = 1.f;
         }
         const float inv = rsqrtf(d);
-        if (lane == j) { a[j] = d * inv; dinv[j] = inv; }
-        if (lane > j) a[j] *= inv;
+        const float lj = (lane == j) ? d * inv : a[j] * inv;  // L(lane, j)
+        const float ljs = lj * inv;                             // L(lane, j) / sqrt(d)
+        if (lane == j) dinv[j] = inv;
+        a[j] = (lane >= j) ? lj : a[j];
 #pragma unroll
-        for (int c = j + 1; c < DG_B; c++) {
-          const float lcj = __shfl_sync(0xffffffffu, a[j], c);
-          if (lane >= c) a[c] = fmaf(-a[j], lcj, a[c]);
-        }
+        for (int c = j + 1; c < DG_B; c++)  // A(lane, c) -= L(lane, j) L(c, j), L(c, j) = A(c, j) / sqrt(d)
+          if (lane >= c) a[c] = fmaf(-ljs, colb[c], a[c]);
+        __syncwarp();
       }
       if (first_bad < kb && lane == 0) { s_fail = 1; atomicCAS(status, 0, (int)(col0 + k0 + first_bad + 1)); }
 #pragma unroll
@@ -497,18 +484,14 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
   // are the jobs, each a reduction over the block rows jt .. I-1, split across the warps.
   for (int i0 = 0; i0 < LN; i0 += DG_B) {
     const int ib = min(DG_B, LN - i0), I = i0 / DG_B;
-    if (t == 0) {
-      int len[DG_WARPS];
-      for (int j = 0; j < DG_WARPS; j++) len[j] = I - j;
-      dg_plan_all(len, I < DG_WARPS ? I : DG_WARPS, s_job, s_qa, s_qb, s_nch);
-    }
     dg_stage(S, Lw, ldw, i0, i0, ib);
     for (int idx = t; idx < DG_B * DG_B; idx += DG_THREADS) {
       const int r = idx >> 5, c = idx & 31;
       Dk[r * DG_LD + c] = (r < ib && c <= r) ? Lw[(i0 + r) + (i0 + c) * ldw] : 0.f;
     }
     __syncthreads();
-    const int job = s_job[warp], qa = s_qa[warp], qb = s_qb[warp], nch = s_nch[warp];
+    const int4 pw = plan[(nsteps + I) * DG_WARPS + warp];
+    const int job = pw.x, qa = pw.y, qb = pw.z, nch = pw.w;
     if (warp == DG_WARPS - 1) {  // L_II^{-1}: lane c solves L_II x = e_c (concurrently with the chunks)
       float x[DG_B];
 #pragma unroll
@@ -830,12 +813,25 @@ __global__ void k_colmax_abs(const double* V, i64 ld, int n, int r, double* out 
 }
 
 // Row sums of |A| (for ||A||_inf), one thread per row.
-__global__ void k_rowsum_abs(const double* A, i64 lda, int n, double* out) {
-  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// P[slice](row) = sum over the slice's columns of |A(row, c)| (stored FP64 A), for the
+// backward error's ||A||_inf: terms rounded to FP32 on the integer pipe and summed in FP32
+// over runs of 256 columns, the runs added in FP64 (relative error < 2e-5, which the
+// backward error's denominator does not notice; FP64 adds per element would cost ~2 ms
+// per 10^9 elements on this part).
+__global__ void __launch_bounds__(256) k_rowsum_abs(const double* __restrict__ A, i64 lda, i64 n, int kslice,
+                                                    double* __restrict__ P) {
+  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const i64 k0 = (i64)blockIdx.y * kslice;
+  const i64 k1 = min(k0 + kslice, n);
   double s = 0;
-  for (int c = 0; c < n; c++) s += fabs(A[i + (i64)c * lda]);
-  out[i] = s;
+  for (i64 c0 = k0; c0 < k1; c0 += 256) {
+    const i64 c1 = min(k1, c0 + 256);
+    float f = 0.f;
+    for (i64 c = c0; c < c1; c++) f += fabsf(ooc_f64_to_f32(A[row + c * lda]));
+    s += ooc_f32_to_f64(f);
+  }
+  P[(i64)blockIdx.y * n + row] = s;
 }
 
 // R(:, q) -= A(seed) X(:, q) over the columns [blockIdx.y * kslice, ...) of A, with A
@@ -1337,7 +1333,8 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     if (m > 0) {
       float* Pn = Djj + LN;
       if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
-      k_colsolve_f32<<<(unsigned)((m + FB - 1) / FB), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN, F->status);
+      k_colsolve_f32<<<(unsigned)((m + CS_ROWS - 1) / CS_ROWS), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN,
+                                                                              F->status);
       OOC_CUDA_TRY(cudaGetLastError());
       if (prof->on) {
         prof->mark(s0);
@@ -1658,6 +1655,33 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     for (int q = 0; q < cols; q++) out[q] = host_max(hv, cols, q, nred);
     return OOC_OK;
   };
+  // The FP32 triangular solve on Rf is ~4 launches per block step: captured once into a
+  // CUDA graph and replayed for X0 and every correction (launch-bound otherwise).
+  cudaGraphExec_t solve_graph = nullptr;
+  bool graph_failed = false;
+  auto solve32 = [&]() -> int {
+    if (!solve_graph && !graph_failed) {
+      cudaGraph_t g = nullptr;
+      int crc = OOC_OK;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        crc = OOC_ERR_CUDA;
+      } else {
+        crc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, nullptr);
+        if (cudaStreamEndCapture(s, &g) != cudaSuccess) crc = OOC_ERR_CUDA;
+      }
+      if (!crc && cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess) {
+        solve_graph = nullptr;
+        crc = OOC_ERR_CUDA;
+      }
+      if (g) cudaGraphDestroy(g);
+      if (crc) {  // capture not available: launch directly from now on
+        cudaGetLastError();
+        graph_failed = true;
+      }
+    }
+    if (solve_graph) return cudaGraphLaunch(solve_graph, s) == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+    return solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+  };
   // ||A||_inf
   double normA = 0;
   {
@@ -1668,7 +1692,11 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
         k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
       }
     } else {
-      k_rowsum_abs<<<gb, 256, 0, s>>>(Astore, lda, (int)n, rows);
+      rc = F->part.ensure((size_t)gslices * n * sizeof(double));
+      if (!rc) {
+        k_rowsum_abs<<<dim3(gb, gslices), 256, 0, s>>>(Astore, lda, n, gks, (double*)F->part.p);
+        k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
+      }
     }
     std::vector<double> nv;
     if (!rc) rc = colmax(rows, n, 1, nv);
@@ -1678,7 +1706,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   if (!rc) rc = colmax(B, ldb, r, nb_);
   if (!rc && F->Lf) {  // X0 from the FP32 factor
     k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, Rf, n, (int)n, r);
-    rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+    rc = solve32();
     if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>(Rf, n, X, ldx, (int)n, r);
   } else if (!rc) {
     OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
@@ -1714,7 +1742,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     if (be <= tol || it >= maxiter) break;
     if (F->Lf) {
       k_to_f32_cols<<<gb, 256, 0, s>>>(R, n, Rf, n, (int)n, r);
-      rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+      rc = solve32();
       if (rc) break;
       k_add_f32_cols<<<gb, 256, 0, s>>>(X, ldx, Rf, n, (int)n, r);
     } else {
@@ -1725,6 +1753,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     it++;
   }
   if (!rc) rc = ooc_wait_stream(h, s);
+  if (solve_graph) cudaGraphExecDestroy(solve_graph);
   cudaFree(R);
   cudaFree(red);
   cudaFree(rows);
