@@ -391,6 +391,332 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------------
+// 256 x 128 blocks: two M=128 accumulators (rows 256 bi2 .. +127 and +128 .. +255) share
+// the B operand, so a stage carries 25 % fewer operand bytes per MMA than two 128 x 128
+// blocks, and the epilogue touches 1 KB (FP32) contiguous runs of each column.  Eight
+// epilogue warps (two per TMEM lane quadrant, 64 columns each) keep all 128 of a thread's C
+// values of the next block in flight while that block's MMAs run.  Used for FP32 C (the
+// working matrix of reduced-precision factors).
+//
+// Blocks are scheduled at run time from a ticket counter (zeroed on the stream before each
+// launch): with the diagonal-tile kernel running beside the update on another stream, the
+// SMs of that kernel's GPC run about 20 % slower, and a static round-robin assignment
+// made the whole launch wait for them.
+// ---------------------------------------------------------------------------------
+constexpr int TM2 = 256;
+constexpr int STAGES2 = 2;
+constexpr int A2_PLANE = TM2 * TK * 2;                    // 32 KB
+constexpr int B2_PLANE = TB * TK * 2;                     // 16 KB
+constexpr int STAGE2_BYTES = 2 * A2_PLANE + 2 * B2_PLANE; // Ahi, Alo, Bhi, Blo
+constexpr int NSLOT2 = 2;                                 // blocks in flight in TMEM
+constexpr int NID2 = 4;                                   // block-index ring entries
+constexpr int TMEM_COLS2 = NSLOT2 * 2 * TB;               // 512: the whole TMEM
+constexpr int EPI2_WARPS = 8;
+constexpr int THREADS2 = 64 + 32 * EPI2_WARPS;
+constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
+static_assert((2 * STAGES2 + 2 * NSLOT2 + 1) * 8 + 8 <= 128, "control block overflow");
+// counters at +128, index ring (2 NID2 barriers + NID2 indices) at +160, all inside the 256
+static_assert(160 + 3 * NID2 * 8 <= 256, "index ring overflow");
+
+// Block t of the block columns [bj_lo, bj_hi) (128 wide) x row blocks bi2 (256 high) with
+// 2 bi2 + 1 >= bj, in strips of STRIP block columns, row by row inside a strip.
+__device__ __forceinline__ void strip2_decode(i64 t, int T, int bj_lo, int bj_hi, int* bi2, int* bj) {
+  const int T2 = (T + 1) / 2;
+  for (int J0 = bj_lo; J0 < bj_hi; J0 += STRIP) {
+    const int w = min(STRIP, bj_hi - J0);
+    const int r0 = J0 / 2;
+    const int a = min(w, 2 * r0 + 2 - J0);
+    const int Kt = (w - a + 1) / 2;  // rows with fewer than w blocks
+    const int rows = T2 - r0;
+    const int kt = min(Kt, rows);
+    const i64 tri_full = (i64)Kt * a + (i64)Kt * (Kt - 1);
+    const i64 cnt = (i64)kt * a + (i64)kt * (kt - 1) + (i64)max(0, rows - Kt) * w;
+    if (t < cnt) {
+      int k, c;
+      if (t < tri_full) {  // k^2 + (a-1) k <= t
+        k = (int)((-(float)(a - 1) + sqrtf((float)((a - 1) * (a - 1)) + 4.f * (float)t)) * 0.5f);
+        while ((i64)(k + 1) * (k + 1) + (i64)(a - 1) * (k + 1) <= t) k++;
+        while ((i64)k * k + (i64)(a - 1) * k > t) k--;
+        c = (int)(t - ((i64)k * k + (i64)(a - 1) * k));
+      } else {
+        const i64 u = t - tri_full;
+        k = (int)(Kt + u / w);
+        c = (int)(u % w);
+      }
+      *bi2 = r0 + k;
+      *bj = J0 + c;
+      return;
+    }
+    t -= cnt;
+  }
+  *bi2 = *bj = 0;  // not reached for t < number of blocks
+}
+
+template <typename TC>
+__global__ void __launch_bounds__(THREADS2, 1)
+    k_syrk2_bf16x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
+                   const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
+                   TC* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
+                   unsigned long long* __restrict__ tickets, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
+  uint64_t* empty = full + STAGES2;
+  uint64_t* tfull = empty + STAGES2;
+  uint64_t* tempty = tfull + NSLOT2;
+  uint64_t* done = tempty + NSLOT2;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  volatile long long* n_issued = (volatile long long*)(smem + STAGES2 * STAGE2_BYTES + 128);
+  volatile long long* n_consumed = n_issued + 1;
+  // block-index ring: the producer publishes each block it starts (-1: no more blocks)
+  uint64_t* idfull = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + 160);
+  uint64_t* idempty = idfull + NID2;
+  volatile long long* ids = (volatile long long*)(idempty + NID2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = Kp / TK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES2; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < NSLOT2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], EPI2_WARPS);
+    }
+    for (int a = 0; a < NID2; a++) {
+      mbar_init(&idfull[a], 1);
+      mbar_init(&idempty[a], 1 + EPI2_WARPS);  // the MMA thread and every epilogue warp
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    *n_issued = 0;
+    *n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS2));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---- TMA producer (lane 0; the warp stays converged around it).  Blocks are handed out
+    // at run time: a CTA's first block is blockIdx.x, each later one gridDim.x + the next
+    // ticket of the launch's counter, so that CTAs slowed by other work beside them (a
+    // kernel on another stream shares their GPC's path to L2) take fewer blocks instead of
+    // holding back the end of the launch.  Every block started is published in the ring.
+    long long c = 0;
+    bool ok = true;
+    i64 t = blockIdx.x;
+    for (int tl = 0; ok; tl++) {
+      const i64 tp = t < nblk ? t : -1;
+      if (lane == 0) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idempty[r], (uint32_t)(((tl / NID2) & 1) ^ 1), abort_flag)) {
+          ok = false;
+        } else {
+          ids[r] = tp;
+          mbar_arrive(&idfull[r]);
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok || tp < 0) break;
+      int bi2, bj;
+      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+      const bool b_in_a = (bj == 2 * bi2 || bj == 2 * bi2 + 1);  // B is one half of A
+      for (int kc = 0; kc < nk; kc++, c++) {
+        if (lane == 0) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+            ok = false;
+          } else {
+            uint8_t* st = smem + s * STAGE2_BYTES;
+            mbar_expect_tx(&full[s], b_in_a ? 2 * A2_PLANE : STAGE2_BYTES);
+            tma_load_2d(st, &map_ahi, &full[s], kc * TK, bi2 * TM2);
+            tma_load_2d(st + A2_PLANE, &map_alo, &full[s], kc * TK, bi2 * TM2);
+            if (!b_in_a) {
+              tma_load_2d(st + 2 * A2_PLANE, &map_bhi, &full[s], kc * TK, bj * TB);
+              tma_load_2d(st + 2 * A2_PLANE + B2_PLANE, &map_blo, &full[s], kc * TK, bj * TB);
+            }
+            *n_issued = c + 1;
+          }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+      }
+      if (!ok) break;
+      unsigned long long nx = 0;
+      if (lane == 0) nx = atomicAdd(tickets, 1ull);
+      nx = __shfl_sync(0xffffffffu, nx, 0);
+      t = (i64)gridDim.x + (i64)nx;
+    }
+    if (!ok && lane == 0) *abort_flag = 1;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: per stage and K-step, three products into each active half
+      long long c = 0;
+      bool ok = true;
+      for (int tl = 0;; tl++) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idfull[r], (uint32_t)((tl / NID2) & 1), abort_flag)) { ok = false; break; }
+        const i64 t = ids[r];
+        mbar_arrive(&idempty[r]);
+        if (t < 0) break;
+        int bi2, bj;
+        strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+        const bool act0 = (2 * bi2 < T) && (2 * bi2 >= bj), act1 = (2 * bi2 + 1 < T) && (2 * bi2 + 1 >= bj);
+        const int slot = tl % NSLOT2;
+        if (!mbar_wait(&tempty[slot], (uint32_t)(((tl / NSLOT2) & 1) ^ 1), abort_flag)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        const uint32_t d0 = tmem + (uint32_t)(slot * 2 * TB), d1 = d0 + (uint32_t)TB;
+        for (int kc = 0; kc < nk; kc++, c++) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
+          *n_consumed = c + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+          const uint32_t base = smem_u32(smem + s * STAGE2_BYTES);
+          const uint32_t a_hi = base, a_lo = base + A2_PLANE;
+          const uint32_t half_b = (uint32_t)(TB * 128);  // 128 rows x 128 bytes
+          uint32_t b_hi = base + 2 * A2_PLANE, b_lo = base + 2 * A2_PLANE + B2_PLANE;
+          if (bj == 2 * bi2) { b_hi = a_hi; b_lo = a_lo; }
+          if (bj == 2 * bi2 + 1) { b_hi = a_hi + half_b; b_lo = a_lo + half_b; }
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; kk++) {
+            const uint32_t off = kk * 32;
+            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+            if (act0) {
+              umma_bf16(d0, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_hi + off), acc0);
+              umma_bf16(d0, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_lo + off), 1u);
+              umma_bf16(d0, umma_desc_sw128(a_lo + off), umma_desc_sw128(b_hi + off), 1u);
+            }
+            if (act1) {
+              umma_bf16(d1, umma_desc_sw128(a_hi + half_b + off), umma_desc_sw128(b_hi + off), acc0);
+              umma_bf16(d1, umma_desc_sw128(a_hi + half_b + off), umma_desc_sw128(b_lo + off), 1u);
+              umma_bf16(d1, umma_desc_sw128(a_lo + half_b + off), umma_desc_sw128(b_hi + off), 1u);
+            }
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[slot]);
+      }
+      if (!ok) *abort_flag = 1;
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 of both halves, 64 columns
+    const int quad = warp & 3;
+    const int cg = ((warp - 2) >> 2) * 64;
+    int bi2 = 0, bj = 0;
+    TC cv[2][64];
+    // index of the CTA's u-th block from the ring: -1 when none is left, -2 on abort
+    auto next_id = [&](int u) -> i64 {
+      const int r = u % NID2;
+      const bool got = mbar_wait(&idfull[r], (uint32_t)((u / NID2) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) return -2;
+      const i64 v = ids[r];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&idempty[r]);
+      return v;
+    };
+    auto load_c = [&](int bi2_, int bj_) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int blk = 2 * bi2_ + h;
+        const int row = blk * TB + quad * 32 + lane, c0 = bj_ * TB + cg;
+        const bool live = (blk < T) && (blk >= bj_) && row < m;
+        const TC* base = C + row + (i64)c0 * ldc;
+#pragma unroll
+        for (int q = 0; q < 64; q++) {
+          const int col = c0 + q;
+          cv[h][q] = (live && col < m && (blk != bj_ || col <= row)) ? base[(i64)q * ldc] : TC(0);
+        }
+      }
+    };
+    i64 t = next_id(0);
+    if (t >= 0) {
+      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+      load_c(bi2, bj);
+    }
+    for (int tl = 0; t >= 0; tl++) {
+      const int slot = tl % NSLOT2;
+      const bool got = mbar_wait(&tfull[slot], (uint32_t)((tl / NSLOT2) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {
+        t = -2;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int blk = 2 * bi2 + h;
+        const bool live = (blk < T) && (blk >= bj);
+        const int row = blk * TB + quad * 32 + lane, c0 = bj * TB + cg;
+        TC* base = C + row + (i64)c0 * ldc;
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + h * TB + cg);
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+          uint32_t v[16];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+              : "r"(taddr + (uint32_t)(16 * ch)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+          if (live && row < m) {
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+              const int col = c0 + 16 * ch + q;
+              if (col < m && (blk != bj || col <= row))
+                base[(i64)(16 * ch + q) * ldc] = cv[h][16 * ch + q] - (TC)__uint_as_float(v[q]);
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[slot]);  // both halves read: the slot may be reused
+      const i64 tn = next_id(tl + 1);
+      if (tn >= 0) {
+        strip2_decode(tn, T, bj_lo, bj_hi, &bi2, &bj);
+        load_c(bi2, bj);
+      }
+      t = tn;
+    }
+    if (t == -2 && lane == 0) *abort_flag = 1;
+  }
+
+  // ---- teardown (as in k_syrk_bf16x3)
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (*abort_flag) {
+    if (threadIdx.x == 0) atomicCAS(status, 0, ERR_TIMEOUT_CODE);
+    if (warp == 1 && lane == 0) {
+      umma_commit(done);
+      (void)mbar_wait(done, 0, nullptr);
+    }
+    if (warp == 0 && lane == 0) {
+      for (long long c = *n_consumed; c < *n_issued; c++)
+        (void)mbar_wait(&full[c % STAGES2], (uint32_t)((c / STAGES2) & 1), nullptr);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS2));
+  }
+}
+
 // ------------------------------ host: tensor maps --------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
@@ -406,15 +732,31 @@ int get_encode() {
   return g_encode ? OOC_OK : OOC_ERR_UNSUPPORTED;
 }
 
-int make_map(CUtensorMap* map, void* base, int Mp, int Kp) {
+int make_map(CUtensorMap* map, void* base, int Mp, int Kp, int box_rows = TB) {
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Mp};
   cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)TB};
+  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
+}
+
+// Number of 256 x 128 blocks of k_syrk2_bf16x3 for block columns [bj_lo, bj_hi).
+i64 count_blocks2(int T, int bj_lo, int bj_hi) {
+  const int T2 = (T + 1) / 2;
+  i64 total = 0;
+  for (int J0 = bj_lo; J0 < bj_hi; J0 += STRIP) {
+    const int w = std::min(STRIP, bj_hi - J0);
+    const int r0 = J0 / 2;
+    const int a = std::min(w, 2 * r0 + 2 - J0);
+    const int Kt = (w - a + 1) / 2;
+    const int rows = T2 - r0;
+    const int kt = std::min(Kt, rows);
+    total += (i64)kt * a + (i64)kt * (kt - 1) + (i64)std::max(0, rows - Kt) * w;
+  }
+  return total;
 }
 
 }  // namespace
@@ -457,6 +799,24 @@ int launch_syrk_t(const TX* X, i64 ldx, TC* C, i64 ldc, int m, int K, const int*
   int dev = 0, nsm = 0;
   OOC_CUDA_TRY(cudaGetDevice(&dev));
   OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if constexpr (sizeof(TC) == 4) {  // FP32 trailing matrix: 256 x 128 blocks
+    CUtensorMap ah, al;
+    if (make_map(&ah, hi, Mp, Kp, TM2) || make_map(&al, lo, Mp, Kp, TM2)) {
+      ooc_set_last_message("cuTensorMapEncodeTiled failed for the BF16 split planes");
+      return OOC_ERR_CUDA;
+    }
+    const i64 nblk2 = count_blocks2((int)T, bj_lo, bj_hi);
+    if (nblk2 <= 0) return OOC_OK;
+    OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk2_bf16x3<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+    const i64 grid2 = std::max<i64>(1, std::min<i64>(nblk2, std::max(1, nsm - std::max(0, reserve_sms))));
+    // the launch's block tickets live in the 256 bytes after the two planes
+    unsigned long long* tickets = reinterpret_cast<unsigned long long*>(lo + (size_t)Mp * Kp);
+    OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
+    k_syrk2_bf16x3<TC><<<(unsigned)grid2, THREADS2, SMEM2_BYTES, s>>>(ah, al, mh, ml, C, ldc, m, Kp, (int)T, bj_lo,
+                                                                     bj_hi, nblk2, tickets, const_cast<int*>(status));
+    OOC_CUDA_TRY(cudaGetLastError());
+    return OOC_OK;
+  }
   const i64 grid = std::max<i64>(1, std::min<i64>(nblk, std::max(1, nsm - std::max(0, reserve_sms))));
   k_syrk_bf16x3<TC><<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo, bj_hi, nblk,
                                                             const_cast<int*>(status));
