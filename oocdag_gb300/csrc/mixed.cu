@@ -12,6 +12,7 @@
 // untouched FP64 matrix, refining the solution until the normwise backward error
 // ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches the requested tolerance.
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -349,9 +350,16 @@ __device__ __forceinline__ void dg_stage(float* __restrict__ S, const float* Lw,
   }
 }
 
+// hi/lo BF16 split of one element of the inverse (the tensor-core column solve's operand)
+__device__ __forceinline__ void dg_split_store(__nv_bfloat16* Xh, __nv_bfloat16* Xl, i64 idx, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  Xh[idx] = h;
+  Xl[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
 __global__ void __launch_bounds__(DG_THREADS, 1)
     k_diag_f32(float* D, i64 ldd, int LN, i64 col0, float* __restrict__ Dinv, i64 lde, float* __restrict__ Xr,
-               int* status) {
+               __nv_bfloat16* __restrict__ Xh, __nv_bfloat16* __restrict__ Xl, int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(16) float dsm[];
   float* S = dsm;                      // staged rows, q-major: S[q * 32 + r]
@@ -536,6 +544,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
         if (r < ib) {
           Xr[(i0 + r) * ldx + j] = y[r];
           Dinv[j + (i64)(i0 + r) * lde] = y[r];
+          if (Xh) dg_split_store(Xh, Xl, (i0 + r) * ldx + j, y[r]);
         }
     }
     if (t >= i0 && t < LN) {
@@ -546,6 +555,7 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
           const float y = (c < ib && r >= c) ? Li[r * DG_LD + c] : 0.f;
           Xr[(i0 + r) * ldx + t] = y;
           Dinv[t + (i64)(i0 + r) * lde] = y;
+          if (Xh) dg_split_store(Xh, Xl, (i0 + r) * ldx + t, y);
         }
     }
     __syncthreads();
@@ -931,6 +941,9 @@ int launch_syrk_bf16x3_f32(const float* X, i64 ldx, float* C, i64 ldc, int m, in
                            cudaStream_t s, void* work, size_t work_bytes, int bj_lo, int bj_hi, int do_split,
                            int reserve_sms);
 size_t bf16x3_work_bytes(int m, int K);
+int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, size_t work_bytes, cudaStream_t s);
+int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xplanes, float* P, i64 ldp, int m, int K,
+                           void* swork, size_t sbytes, const int* status, cudaStream_t s);
 
 namespace {
 
@@ -1158,6 +1171,7 @@ struct ooc_factor {
   int* status = nullptr;   // device status word of the factorization
   int info = 0;
   DevBuf part, partf, work, scratch;
+  DevBuf work2;  // BF16 planes of the panel before its tensor-core column solve
   ~ooc_factor() {
     if (L) cudaFree(L);
     if (Dinv) cudaFree(Dinv);
@@ -1292,9 +1306,15 @@ int factor_mixed(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int6
 //   s1: the diagonal tile's Cholesky and inverse in one FP32 CTA (k_diag_f32), beside the
 //       bulk update of the previous panel (the persistent tensor-core update leaves
 //       kChainSMs SMs free for it);
-//   s0: the column solve (FP32 product with the inverse, in place, every SM), then the
-//       trailing update in `prec` -- the next panel's block columns first (an event lets
-//       s1 start on its diagonal tile), then the rest.
+//   s0: the column solve (product with the inverse), then the trailing update in `prec` --
+//       the next panel's block columns first (an event lets s1 start on its diagonal
+//       tile), then the rest.
+// Split-BF16 factors with nb a multiple of 128 solve the panel on the tensor cores
+// (k_trsm2_bf16x3, the update's three products): the panel is split into BF16 planes
+// while its diagonal tile is factored (right after the previous narrow update, on s0),
+// the diagonal kernel also writes the planes of the inverse, and the solve writes the FP32
+// panel together with the planes the update reads.  Otherwise the solve is an FP32
+// product on the CUDA cores (k_colsolve_f32) and the update splits the panel itself.
 constexpr int kChainSMs = 1;  // the diagonal kernel is one CTA
 
 int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
@@ -1305,10 +1325,17 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
   const i64 lda = F->ld;
   const i64 tile = (i64)nb * nb;
   if (nb > DG_MAX) return OOC_ERR_UNSUPPORTED;
-  int rc = F->scratch.ensure((size_t)tile * sizeof(float));
+  const bool split = (nb % 128 == 0);
+  const bool tc_solve = split && prec == OOC_PREC_BF16X3 && n > nb;
+  int rc = F->scratch.ensure((size_t)tile * (sizeof(float) + (tc_solve ? 2 * sizeof(__nv_bfloat16) : 0)));
   if (rc) return rc;
   float* Xr = (float*)F->scratch.p;  // L_jj^{-1}, row-major (ld LN), from the diagonal kernel
-  const bool split = (nb % 128 == 0);
+  __nv_bfloat16* Xh = tc_solve ? reinterpret_cast<__nv_bfloat16*>(Xr + tile) : nullptr;  // its hi, lo planes
+  __nv_bfloat16* Xl = tc_solve ? Xh + tile : nullptr;
+  if (tc_solve) {  // planes of the panel before (work2) and after (work) the solve
+    const size_t pb = bf16x3_work_bytes((int)(n - nb), nb);
+    if ((rc = F->work.ensure(pb)) || (rc = F->work2.ensure(pb))) return rc;
+  }
   OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
   cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: diagonal tile done (s1 -> s0)
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
@@ -1318,13 +1345,18 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
   } guard{evA, evP};
   OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
+  if (tc_solve) {  // panel 0 below its diagonal tile, beside the first diagonal kernel
+    rc = launch_split_bf16_f32(A + nb, lda, (int)(n - nb), nb, F->work2.p, F->work2.bytes, s0);
+    if (rc) return rc;
+  }
   for (int j = 0; j < bb; j++) {
     const i64 J0 = (i64)j * nb;
     const int LN = (int)std::min<i64>(nb, n - J0);
     float* Djj = A + J0 + J0 * lda;
     OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
     if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, nb, Xr, F->status);
+    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, nb, Xr, Xh, Xl,
+                                               F->status);
     OOC_CUDA_TRY(cudaGetLastError());
     if (prof->on) prof->mark(s1);
     OOC_CUDA_TRY(cudaEventRecord(evP, s1));
@@ -1333,9 +1365,15 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     if (m > 0) {
       float* Pn = Djj + LN;
       if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
-      k_colsolve_f32<<<(unsigned)((m + CS_ROWS - 1) / CS_ROWS), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN,
-                                                                              F->status);
-      OOC_CUDA_TRY(cudaGetLastError());
+      if (tc_solve) {
+        rc = launch_trsm_bf16x3_f32(F->work2.p, F->work2.bytes, Xh, Pn, lda, (int)m, LN, F->work.p, F->work.bytes,
+                                    F->status, s0);
+        if (rc) return rc;
+      } else {
+        k_colsolve_f32<<<(unsigned)((m + CS_ROWS - 1) / CS_ROWS), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN,
+                                                                                F->status);
+        OOC_CUDA_TRY(cudaGetLastError());
+      }
       if (prof->on) {
         prof->mark(s0);
         prof->mark(s0);
@@ -1343,7 +1381,18 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
         prof->flops.push_back((double)m * (double)(m + 1) * LN);
       }
       float* C = A + (J0 + LN) * (1 + lda);
-      if (split) {
+      if (tc_solve) {  // the planes come from the solve
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 0, 0);
+        if (rc) return rc;
+        OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+        // panel j+1 is final now: its planes (rows below its diagonal tile; it is nb wide
+        // whenever rows remain below it), then the bulk of the update
+        if (m - nb > 0) {
+          rc = launch_split_bf16_f32(C + nb, lda, (int)(m - nb), nb, F->work2.p, F->work2.bytes, s0);
+          if (rc) return rc;
+        }
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
+      } else if (split) {
         rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1, 0);
         if (rc) return rc;
         OOC_CUDA_TRY(cudaEventRecord(evA, s0));
@@ -1503,7 +1552,11 @@ extern "C" int64_t ooc_factor_bytes(int64_t n, int nb, int prec) {
   int64_t b = (int64_t)nb * 16 * 8 + 256;  // tmp, status
   if (prec == OOC_PREC_FP64) return b + n * n * 8 + bb * nb * nb * 8 + n * nb * 8 + (int64_t)nb * nb * 8;
   b += n * n * 4 + bb * nb * nb * 4 + (int64_t)nb * 16 * 4 + 2 * (int64_t)nb * nb * 4;  // Lf, Dinvf, tmpf, scratch
-  if (prec == OOC_PREC_BF16X3) b += 2 * ((n + 127) / 128 * 128) * ((nb + 63) / 64 * 64) * 2;  // split planes
+  if (prec == OOC_PREC_BF16X3) {
+    const int64_t planes = 2 * ((n + 127) / 128 * 128) * ((nb + 63) / 64 * 64) * 2 + 256;  // hi + lo
+    b += planes;
+    if (nb % 128 == 0 && n > nb) b += planes + 2 * (int64_t)nb * nb * 2;  // tensor-core column solve
+  }
   return b;
 }
 

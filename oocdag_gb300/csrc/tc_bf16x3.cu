@@ -717,6 +717,255 @@ __global__ void __launch_bounds__(THREADS2, 1)
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Column solve of a panel on the tensor cores: P = U X^T (m x nb), U the panel before the
+// solve and X = L_jj^{-1} (lower triangular), both given as BF16 hi/lo planes (K-major),
+// with the update's three products.  Block t = (row tile bi2 of 256 rows, column block cb
+// of 128): K runs over [0, 128 (cb + 1)) only, since X(c, k) = 0 for k > c.  The epilogue
+// writes the FP32 result into the panel (column-major, ld ldp) and its hi/lo split into the
+// planes the trailing update reads (Mp x Kp, row-major), so the update needs no split pass.
+// Same roles, rings, bounded waits, run-time block tickets and teardown as k_syrk2_bf16x3.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(THREADS2, 1)
+    k_trsm2_bf16x3(const __grid_constant__ CUtensorMap map_uhi, const __grid_constant__ CUtensorMap map_ulo,
+                   const __grid_constant__ CUtensorMap map_xhi, const __grid_constant__ CUtensorMap map_xlo,
+                   float* __restrict__ P, i64 ldp, __nv_bfloat16* __restrict__ shi, __nv_bfloat16* __restrict__ slo,
+                   int Kp, int m, int ncb, i64 nblk, unsigned long long* __restrict__ tickets, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
+  uint64_t* empty = full + STAGES2;
+  uint64_t* tfull = empty + STAGES2;
+  uint64_t* tempty = tfull + NSLOT2;
+  uint64_t* done = tempty + NSLOT2;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  volatile long long* n_issued = (volatile long long*)(smem + STAGES2 * STAGE2_BYTES + 128);
+  volatile long long* n_consumed = n_issued + 1;
+  uint64_t* idfull = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + 160);
+  uint64_t* idempty = idfull + NID2;
+  volatile long long* ids = (volatile long long*)(idempty + NID2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES2; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < NSLOT2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], EPI2_WARPS);
+    }
+    for (int a = 0; a < NID2; a++) {
+      mbar_init(&idfull[a], 1);
+      mbar_init(&idempty[a], 1 + EPI2_WARPS);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    *n_issued = 0;
+    *n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS2));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---- TMA producer (lane 0; the warp stays converged around it)
+    long long c = 0;
+    bool ok = true;
+    i64 t = blockIdx.x;
+    for (int tl = 0; ok; tl++) {
+      const i64 tp = t < nblk ? t : -1;
+      if (lane == 0) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idempty[r], (uint32_t)(((tl / NID2) & 1) ^ 1), abort_flag)) {
+          ok = false;
+        } else {
+          ids[r] = tp;
+          mbar_arrive(&idfull[r]);
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok || tp < 0) break;
+      const int bi2 = (int)(t / ncb), cb = (int)(t % ncb);
+      const int nk = 2 * (cb + 1);
+      for (int kc = 0; kc < nk; kc++, c++) {
+        if (lane == 0) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+            ok = false;
+          } else {
+            uint8_t* st = smem + s * STAGE2_BYTES;
+            mbar_expect_tx(&full[s], STAGE2_BYTES);
+            tma_load_2d(st, &map_uhi, &full[s], kc * TK, bi2 * TM2);
+            tma_load_2d(st + A2_PLANE, &map_ulo, &full[s], kc * TK, bi2 * TM2);
+            tma_load_2d(st + 2 * A2_PLANE, &map_xhi, &full[s], kc * TK, cb * TB);
+            tma_load_2d(st + 2 * A2_PLANE + B2_PLANE, &map_xlo, &full[s], kc * TK, cb * TB);
+            *n_issued = c + 1;
+          }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+      }
+      if (!ok) break;
+      unsigned long long nx = 0;
+      if (lane == 0) nx = atomicAdd(tickets, 1ull);
+      nx = __shfl_sync(0xffffffffu, nx, 0);
+      t = (i64)gridDim.x + (i64)nx;
+    }
+    if (!ok && lane == 0) *abort_flag = 1;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      long long c = 0;
+      bool ok = true;
+      for (int tl = 0;; tl++) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idfull[r], (uint32_t)((tl / NID2) & 1), abort_flag)) { ok = false; break; }
+        const i64 t = ids[r];
+        mbar_arrive(&idempty[r]);
+        if (t < 0) break;
+        const int bi2 = (int)(t / ncb), cb = (int)(t % ncb);
+        const int nk = 2 * (cb + 1);
+        const bool act1 = (2 * bi2 + 1) * TB < m;
+        const int slot = tl % NSLOT2;
+        if (!mbar_wait(&tempty[slot], (uint32_t)(((tl / NSLOT2) & 1) ^ 1), abort_flag)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        const uint32_t d0 = tmem + (uint32_t)(slot * 2 * TB), d1 = d0 + (uint32_t)TB;
+        for (int kc = 0; kc < nk; kc++, c++) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
+          *n_consumed = c + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+          const uint32_t base = smem_u32(smem + s * STAGE2_BYTES);
+          const uint32_t a_hi = base, a_lo = base + A2_PLANE;
+          const uint32_t half_a = (uint32_t)(TB * 128);  // 128 rows x 128 bytes
+          const uint32_t b_hi = base + 2 * A2_PLANE, b_lo = base + 2 * A2_PLANE + B2_PLANE;
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; kk++) {
+            const uint32_t off = kk * 32;
+            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+            umma_bf16(d0, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_hi + off), acc0);
+            umma_bf16(d0, umma_desc_sw128(a_hi + off), umma_desc_sw128(b_lo + off), 1u);
+            umma_bf16(d0, umma_desc_sw128(a_lo + off), umma_desc_sw128(b_hi + off), 1u);
+            if (act1) {
+              umma_bf16(d1, umma_desc_sw128(a_hi + half_a + off), umma_desc_sw128(b_hi + off), acc0);
+              umma_bf16(d1, umma_desc_sw128(a_hi + half_a + off), umma_desc_sw128(b_lo + off), 1u);
+              umma_bf16(d1, umma_desc_sw128(a_lo + half_a + off), umma_desc_sw128(b_hi + off), 1u);
+            }
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[slot]);
+      }
+      if (!ok) *abort_flag = 1;
+    }
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 of both halves, 64 columns;
+    // a thread owns one row: FP32 stores coalesce along the column, and each plane gets
+    // 32-byte runs of the row.
+    const int quad = warp & 3;
+    const int cg = ((warp - 2) >> 2) * 64;
+    auto next_id = [&](int u) -> i64 {
+      const int r = u % NID2;
+      const bool got = mbar_wait(&idfull[r], (uint32_t)((u / NID2) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) return -2;
+      const i64 v = ids[r];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&idempty[r]);
+      return v;
+    };
+    i64 t = next_id(0);
+    for (int tl = 0; t >= 0; tl++) {
+      const int bi2 = (int)(t / ncb), cb = (int)(t % ncb);
+      const int slot = tl % NSLOT2;
+      const bool got = mbar_wait(&tfull[slot], (uint32_t)((tl / NSLOT2) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {
+        t = -2;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if ((2 * bi2 + h) * TB >= m) continue;  // uniform: this half was not computed
+        const int row = (2 * bi2 + h) * TB + quad * 32 + lane, c0 = cb * TB + cg;
+        float* pb = P + row + (i64)c0 * ldp;
+        __nv_bfloat16* hb = shi + (i64)row * Kp + c0;
+        __nv_bfloat16* lb = slo + (i64)row * Kp + c0;
+        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + h * TB + cg);
+#pragma unroll
+        for (int ch = 0; ch < 4; ch++) {
+          uint32_t v[16];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+              : "r"(taddr + (uint32_t)(16 * ch)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+          if (row < m) {
+            uint32_t ph[8], pl[8];
+#pragma unroll
+            for (int q = 0; q < 16; q += 2) {
+              const float f0 = __uint_as_float(v[q]), f1 = __uint_as_float(v[q + 1]);
+              pb[(i64)(16 * ch + q) * ldp] = f0;
+              pb[(i64)(16 * ch + q + 1) * ldp] = f1;
+              const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+              const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
+              const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
+              ph[q / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+              pl[q / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+            }
+            uint4* h4 = reinterpret_cast<uint4*>(hb + 16 * ch);
+            uint4* l4 = reinterpret_cast<uint4*>(lb + 16 * ch);
+            h4[0] = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+            h4[1] = make_uint4(ph[4], ph[5], ph[6], ph[7]);
+            l4[0] = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+            l4[1] = make_uint4(pl[4], pl[5], pl[6], pl[7]);
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[slot]);
+      t = next_id(tl + 1);
+    }
+    if (t == -2 && lane == 0) *abort_flag = 1;
+  }
+
+  // ---- teardown (as in k_syrk_bf16x3)
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (*abort_flag) {
+    if (threadIdx.x == 0) atomicCAS(status, 0, ERR_TIMEOUT_CODE);
+    if (warp == 1 && lane == 0) {
+      umma_commit(done);
+      (void)mbar_wait(done, 0, nullptr);
+    }
+    if (warp == 0 && lane == 0) {
+      for (long long c = *n_consumed; c < *n_issued; c++)
+        (void)mbar_wait(&full[c % STAGES2], (uint32_t)((c / STAGES2) & 1), nullptr);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS2));
+  }
+}
+
 // ------------------------------ host: tensor maps --------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
@@ -837,4 +1086,60 @@ int launch_syrk_bf16x3_f32(const float* X, i64 ldx, float* C, i64 ldc, int m, in
                            int reserve_sms) {
   return launch_syrk_t<float, float>(X, ldx, C, ldc, m, K, status, s, work, work_bytes, bj_lo, bj_hi, do_split,
                                      reserve_sms);
+}
+
+// FP32 panel X (m x K, column-major, ld ldx) -> BF16 hi/lo planes at `work` (the layout of
+// bf16x3_work_bytes(m, K): Mp x Kp row-major hi, then lo, zero-padded).
+int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, size_t work_bytes, cudaStream_t s) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (work_bytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
+  const int Mp = (m + TB - 1) / TB * TB;
+  const int Kp = (K + TK - 1) / TK * TK;
+  __nv_bfloat16* hi = (__nv_bfloat16*)work;
+  __nv_bfloat16* lo = hi + (size_t)Mp * Kp;
+  k_split_bf16<float><<<dim3((unsigned)(Kp / 32), (unsigned)(Mp / 32)), dim3(32, 8), 0, s>>>(X, ldx, hi, lo, m, K, Mp,
+                                                                                          Kp);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+// Column solve of an FP32 panel on the tensor cores, P = U X^T (k_trsm2_bf16x3).  `uwork`
+// holds the planes of the panel before the solve (launch_split_bf16_f32, m x K) followed by
+// the 256 bytes of block tickets; `xplanes` the hi then lo planes of X = L_jj^{-1} (K x K,
+// row-major).  The result goes to P (ld ldp) and, split, to the planes at `swork` in the
+// layout launch_syrk_bf16x3_f32 reads with do_split = 0.  K must be a multiple of 128.
+int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xplanes, float* P, i64 ldp, int m, int K,
+                           void* swork, size_t sbytes, const int* status, cudaStream_t s) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (K % TB != 0) return OOC_ERR_UNSUPPORTED;
+  if (!status || !uwork || !xplanes || !swork) return OOC_ERR_INTERNAL;
+  if (ubytes < bf16x3_work_bytes(m, K) || sbytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
+  int rc = get_encode();
+  if (rc) return rc;
+  const int Mp = (m + TB - 1) / TB * TB, Kp = K;
+  __nv_bfloat16* uh = (__nv_bfloat16*)uwork;
+  __nv_bfloat16* ul = uh + (size_t)Mp * Kp;
+  unsigned long long* tickets = reinterpret_cast<unsigned long long*>(ul + (size_t)Mp * Kp);
+  __nv_bfloat16* xh = (__nv_bfloat16*)const_cast<void*>(xplanes);
+  __nv_bfloat16* xl = xh + (size_t)K * K;
+  __nv_bfloat16* sh = (__nv_bfloat16*)swork;
+  __nv_bfloat16* sl = sh + (size_t)Mp * Kp;
+  CUtensorMap mu_h, mu_l, mx_h, mx_l;
+  if (make_map(&mu_h, uh, Mp, Kp, TM2) || make_map(&mu_l, ul, Mp, Kp, TM2) || make_map(&mx_h, xh, K, K, TB) ||
+      make_map(&mx_l, xl, K, K, TB)) {
+    ooc_set_last_message("cuTensorMapEncodeTiled failed for the column-solve planes");
+    return OOC_ERR_CUDA;
+  }
+  const int ncb = K / TB;
+  const i64 nblk = (i64)((Mp + TM2 - 1) / TM2) * ncb;
+  int dev = 0, nsm = 0;
+  OOC_CUDA_TRY(cudaGetDevice(&dev));
+  OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const i64 grid = std::max<i64>(1, std::min<i64>(nblk, nsm));
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm2_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
+  OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
+  k_trsm2_bf16x3<<<(unsigned)grid, THREADS2, SMEM2_BYTES, s>>>(mu_h, mu_l, mx_h, mx_l, P, ldp, sh, sl, Kp, m, ncb,
+                                                              nblk, tickets, const_cast<int*>(status));
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
 }
