@@ -90,6 +90,38 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// C (global, FP32) += box at smem `src`, added in L2 (TMA reduction); coordinates are
+// (row, column) of the box's first element, rows innermost.
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, const void* src, int c0, int c1) {
+  asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.bulk_group [%0, {%2, %3}], [%1];\n" ::"l"(
+                   (uint64_t)map),
+               "r"(smem_u32(src)), "r"(c0), "r"(c1)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// the bulk groups committed so far, all but the newest N, have finished reading shared memory
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t count) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+}
+// barrier over `count` threads that also returns the AND of their predicates
+__device__ __forceinline__ bool named_bar_and(uint32_t id, uint32_t count, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n bar.red.and.pred b, %2, %3, a;\n selp.u32 %0, 1, 0, b;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
 // Shared-memory matrix descriptor: K-major operand in 128-byte-swizzled atoms of
 // 8 rows x 128 bytes (stride between atoms 1024 bytes).
 __device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
@@ -394,10 +426,14 @@ __global__ void __launch_bounds__(THREADS, 1)
 // ---------------------------------------------------------------------------------
 // 256 x 128 blocks: two M=128 accumulators (rows 256 bi2 .. +127 and +128 .. +255) share
 // the B operand, so a stage carries 25 % fewer operand bytes per MMA than two 128 x 128
-// blocks, and the epilogue touches 1 KB (FP32) contiguous runs of each column.  Eight
-// epilogue warps (two per TMEM lane quadrant, 64 columns each) keep all 128 of a thread's C
-// values of the next block in flight while that block's MMAs run.  Used for FP32 C (the
-// working matrix of reduced-precision factors).
+// blocks.  Eight epilogue warps (two per TMEM lane quadrant, 64 columns each) stage -D in
+// shared memory and add it into C with TMA reductions (cp.reduce.async.bulk.tensor .add):
+// the read-modify-write of C happens in L2 on whole 1 KB column runs of a 256-row block,
+// where per-thread loads and stores of one row across 64 columns reached only about half
+// of the HBM bandwidth.  The FP32 additions in L2 round to nearest; like the L2's other
+// FP32 atomics they may flush subnormal values (|x| < 2^-126) to zero.  Used for FP32 C (the
+// working matrix of reduced-precision factors) with a 16-byte-aligned base and leading
+// dimension.
 //
 // Blocks are scheduled at run time from a ticket counter (zeroed on the stream before each
 // launch): with the diagonal-tile kernel running beside the update on another stream, the
@@ -418,6 +454,12 @@ constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
 static_assert((2 * STAGES2 + 2 * NSLOT2 + 1) * 8 + 8 <= 128, "control block overflow");
 // counters at +128, index ring (2 NID2 barriers + NID2 indices) at +160, all inside the 256
 static_assert(160 + 3 * NID2 * 8 <= 256, "index ring overflow");
+// Update epilogue (FP32 C): per column group of four warps, two staging boxes of 256 rows x
+// CB_COLS columns after the control block, handed to TMA reductions.
+constexpr int CB_COLS = 8;
+constexpr int CB_FLOATS = TM2 * CB_COLS;                       // 8 KB
+constexpr int SMEM2U_BYTES = SMEM2_BYTES + 2 * 2 * CB_FLOATS * 4;  // 230,656
+static_assert(SMEM2U_BYTES <= 232448, "update kernel shared memory");
 
 // Block t of the block columns [bj_lo, bj_hi) (128 wide) x row blocks bi2 (256 high) with
 // 2 bi2 + 1 >= bj, in strips of STRIP block columns, row by row inside a strip.
@@ -457,8 +499,9 @@ template <typename TC>
 __global__ void __launch_bounds__(THREADS2, 1)
     k_syrk2_bf16x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                    const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
-                   TC* __restrict__ C, i64 ldc, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
+                   const __grid_constant__ CUtensorMap map_c, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
                    unsigned long long* __restrict__ tickets, int* status) {
+  static_assert(sizeof(TC) == 4, "the reduction epilogue adds into FP32 C");
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -614,84 +657,92 @@ __global__ void __launch_bounds__(THREADS2, 1)
       if (!ok) *abort_flag = 1;
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 of both halves, 64 columns
+    // ---- epilogue: the four warps of a column group (64 columns; warp w reads TMEM lanes
+    // 32 (w % 4) .. +31 of both halves) stage -D in boxes of 256 rows x CB_COLS columns, and
+    // one thread adds each box into C with a TMA reduction: L2 does the read-modify-write in
+    // 1 KB column runs, and the SM keeps no C values.  Elements outside the lower triangle
+    // (above the diagonal in a diagonal block, or a half above it) are staged as -0.0, which
+    // leaves any value unchanged; rows and columns past m are clipped by the tensor map.
+    // Every decision to stop is a vote of the group (bar.red), so that all four warps always
+    // meet the same named barriers.
     const int quad = warp & 3;
-    const int cg = ((warp - 2) >> 2) * 64;
-    int bi2 = 0, bj = 0;
-    TC cv[2][64];
+    const int grp = (warp - 2) >> 2;
+    const int cg = grp * 64;
+    const uint32_t gbar = 1 + (uint32_t)grp;  // named barrier of the column group (128 threads)
+    const bool issuer = (warp == 2 + 4 * grp) && lane == 0;
+    float* cbox = reinterpret_cast<float*>(smem + STAGES2 * STAGE2_BYTES + 256) + grp * 2 * CB_FLOATS;
     // index of the CTA's u-th block from the ring: -1 when none is left, -2 on abort
     auto next_id = [&](int u) -> i64 {
       const int r = u % NID2;
       const bool got = mbar_wait(&idfull[r], (uint32_t)((u / NID2) & 1), abort_flag);
-      if (!__all_sync(0xffffffffu, got)) return -2;
-      const i64 v = ids[r];
+      i64 v = -2;
+      if (__all_sync(0xffffffffu, got)) v = ids[r];
       __syncwarp();
-      if (lane == 0) mbar_arrive(&idempty[r]);
-      return v;
+      if (lane == 0 && v != -2) mbar_arrive(&idempty[r]);
+      return named_bar_and(gbar, 128, v != -2) ? v : -2;
     };
-    auto load_c = [&](int bi2_, int bj_) {
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int blk = 2 * bi2_ + h;
-        const int row = blk * TB + quad * 32 + lane, c0 = bj_ * TB + cg;
-        const bool live = (blk < T) && (blk >= bj_) && row < m;
-        const TC* base = C + row + (i64)c0 * ldc;
-#pragma unroll
-        for (int q = 0; q < 64; q++) {
-          const int col = c0 + q;
-          cv[h][q] = (live && col < m && (blk != bj_ || col <= row)) ? base[(i64)q * ldc] : TC(0);
-        }
-      }
-    };
+    int nbox = 0;
     i64 t = next_id(0);
-    if (t >= 0) {
-      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
-      load_c(bi2, bj);
-    }
     for (int tl = 0; t >= 0; tl++) {
+      int bi2, bj;
+      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
       const int slot = tl % NSLOT2;
       const bool got = mbar_wait(&tfull[slot], (uint32_t)((tl / NSLOT2) & 1), abort_flag);
-      if (!__all_sync(0xffffffffu, got)) {
+      if (!named_bar_and(gbar, 128, __all_sync(0xffffffffu, got))) {
         t = -2;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+      const int r0 = quad * 32 + lane;  // row within a half
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + cg);
+#pragma unroll 1
+      for (int ch = 0; ch < 4; ch++) {
+        uint32_t v0[16], v1[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(v0[0]), "=r"(v0[1]), "=r"(v0[2]), "=r"(v0[3]), "=r"(v0[4]), "=r"(v0[5]), "=r"(v0[6]), "=r"(v0[7]),
+              "=r"(v0[8]), "=r"(v0[9]), "=r"(v0[10]), "=r"(v0[11]), "=r"(v0[12]), "=r"(v0[13]), "=r"(v0[14]),
+              "=r"(v0[15])
+            : "r"(taddr + (uint32_t)(16 * ch)));
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(v1[0]), "=r"(v1[1]), "=r"(v1[2]), "=r"(v1[3]), "=r"(v1[4]), "=r"(v1[5]), "=r"(v1[6]), "=r"(v1[7]),
+              "=r"(v1[8]), "=r"(v1[9]), "=r"(v1[10]), "=r"(v1[11]), "=r"(v1[12]), "=r"(v1[13]), "=r"(v1[14]),
+              "=r"(v1[15])
+            : "r"(taddr + (uint32_t)(TB + 16 * ch)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int blk = 2 * bi2 + h;
-        const bool live = (blk < T) && (blk >= bj);
-        const int row = blk * TB + quad * 32 + lane, c0 = bj * TB + cg;
-        TC* base = C + row + (i64)c0 * ldc;
-        const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + h * TB + cg);
+        for (int sub = 0; sub < 16 / CB_COLS; sub++) {
+          float* box = cbox + (nbox & 1) * CB_FLOATS;
+          if (issuer) bulk_wait_read<1>();  // the reduction that last read this box is done with it
+          named_bar_sync(gbar, 128);
+          const int col0 = bj * TB + cg + 16 * ch + CB_COLS * sub;
 #pragma unroll
-        for (int ch = 0; ch < 4; ch++) {
-          uint32_t v[16];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-              : "r"(taddr + (uint32_t)(16 * ch)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
-          if (live && row < m) {
+          for (int c = 0; c < CB_COLS; c++) {
+            const int col = col0 + c;
 #pragma unroll
-            for (int q = 0; q < 16; q++) {
-              const int col = c0 + 16 * ch + q;
-              if (col < m && (blk != bj || col <= row))
-                base[(i64)(16 * ch + q) * ldc] = cv[h][16 * ch + q] - (TC)__uint_as_float(v[q]);
+            for (int h = 0; h < 2; h++) {
+              const int blk = 2 * bi2 + h, row = blk * TB + r0;
+              const bool keep = blk < T && blk >= bj && (blk != bj || col <= row);
+              const uint32_t u = h ? v1[CB_COLS * sub + c] : v0[CB_COLS * sub + c];
+              box[c * TM2 + h * TB + r0] = keep ? -__uint_as_float(u) : -0.0f;
             }
           }
+          fence_proxy_async_smem();
+          named_bar_sync(gbar, 128);
+          if (issuer) {
+            tma_reduce_add_2d(&map_c, box, bi2 * TM2, col0);
+            bulk_commit();
+          }
+          nbox++;
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[slot]);  // both halves read: the slot may be reused
-      const i64 tn = next_id(tl + 1);
-      if (tn >= 0) {
-        strip2_decode(tn, T, bj_lo, bj_hi, &bi2, &bj);
-        load_c(bi2, bj);
-      }
-      t = tn;
+      t = next_id(tl + 1);
     }
+    if (issuer) bulk_wait_all();  // every reduction of this CTA has landed
     if (t == -2 && lane == 0) *abort_flag = 1;
   }
 
@@ -992,6 +1043,19 @@ int make_map(CUtensorMap* map, void* base, int Mp, int Kp, int box_rows = TB) {
   return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
 }
 
+// FP32 C (m x m, column-major, ld ldc) for the update's TMA reductions: boxes of 256 rows x
+// CB_COLS columns, rows innermost.
+int make_map_c32(CUtensorMap* map, float* C, int m, i64 ldc) {
+  cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)m};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)TM2, (cuuint32_t)CB_COLS};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
+}
+
 // Number of 256 x 128 blocks of k_syrk2_bf16x3 for block columns [bj_lo, bj_hi).
 i64 count_blocks2(int T, int bj_lo, int bj_hi) {
   const int T2 = (T + 1) / 2;
@@ -1048,23 +1112,29 @@ int launch_syrk_t(const TX* X, i64 ldx, TC* C, i64 ldc, int m, int K, const int*
   int dev = 0, nsm = 0;
   OOC_CUDA_TRY(cudaGetDevice(&dev));
   OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  if constexpr (sizeof(TC) == 4) {  // FP32 trailing matrix: 256 x 128 blocks
-    CUtensorMap ah, al;
-    if (make_map(&ah, hi, Mp, Kp, TM2) || make_map(&al, lo, Mp, Kp, TM2)) {
-      ooc_set_last_message("cuTensorMapEncodeTiled failed for the BF16 split planes");
-      return OOC_ERR_CUDA;
+  // FP32 trailing matrix with a 16-byte-aligned base and leading dimension (the TMA
+  // reduction's requirements): 256 x 128 blocks; otherwise the 128 x 128 kernel.
+  if constexpr (sizeof(TC) == 4) {
+    if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && (ldc * (i64)sizeof(TC)) % 16 == 0) {
+      CUtensorMap ah, al, mc;
+      if (make_map(&ah, hi, Mp, Kp, TM2) || make_map(&al, lo, Mp, Kp, TM2) || make_map_c32(&mc, C, m, ldc)) {
+        ooc_set_last_message("cuTensorMapEncodeTiled failed for the update operands");
+        return OOC_ERR_CUDA;
+      }
+      const i64 nblk2 = count_blocks2((int)T, bj_lo, bj_hi);
+      if (nblk2 <= 0) return OOC_OK;
+      OOC_CUDA_TRY(
+          cudaFuncSetAttribute(k_syrk2_bf16x3<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2U_BYTES));
+      const i64 grid2 = std::max<i64>(1, std::min<i64>(nblk2, std::max(1, nsm - std::max(0, reserve_sms))));
+      // the launch's block tickets live in the 256 bytes after the two planes
+      unsigned long long* tickets = reinterpret_cast<unsigned long long*>(lo + (size_t)Mp * Kp);
+      OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
+      k_syrk2_bf16x3<TC><<<(unsigned)grid2, THREADS2, SMEM2U_BYTES, s>>>(ah, al, mh, ml, mc, m, Kp, (int)T, bj_lo,
+                                                                         bj_hi, nblk2, tickets,
+                                                                         const_cast<int*>(status));
+      OOC_CUDA_TRY(cudaGetLastError());
+      return OOC_OK;
     }
-    const i64 nblk2 = count_blocks2((int)T, bj_lo, bj_hi);
-    if (nblk2 <= 0) return OOC_OK;
-    OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk2_bf16x3<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
-    const i64 grid2 = std::max<i64>(1, std::min<i64>(nblk2, std::max(1, nsm - std::max(0, reserve_sms))));
-    // the launch's block tickets live in the 256 bytes after the two planes
-    unsigned long long* tickets = reinterpret_cast<unsigned long long*>(lo + (size_t)Mp * Kp);
-    OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
-    k_syrk2_bf16x3<TC><<<(unsigned)grid2, THREADS2, SMEM2_BYTES, s>>>(ah, al, mh, ml, C, ldc, m, Kp, (int)T, bj_lo,
-                                                                     bj_hi, nblk2, tickets, const_cast<int*>(status));
-    OOC_CUDA_TRY(cudaGetLastError());
-    return OOC_OK;
   }
   const i64 grid = std::max<i64>(1, std::min<i64>(nblk, std::max(1, nsm - std::max(0, reserve_sms))));
   k_syrk_bf16x3<TC><<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, Kp, (int)T, bj_lo, bj_hi, nblk,
