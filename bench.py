@@ -595,7 +595,8 @@ def run_mixed(args):
     share_fac = fac_ms / (ms_local * args.steps)
     bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
     mult = 3 if args.prec == "bf16x3" else 1
-    upd_roof = {"kernel": "k_syrk_bf16x3<float> (persistent split-BF16 tcgen05 trailing update, FP32 C)"
+    upd_roof = {"kernel": "k_syrk2_bf16x3<float> (persistent split-BF16 tcgen05 trailing update, 256x128 blocks, "
+                          "FP32 C updated by TMA reductions)"
                 if args.prec == "bf16x3" else "k_syrk_f32<float> (FP32 FFMA trailing update)",
                 "bound": "tensor" if args.prec == "bf16x3" else "fp32-simt",
                 "achieved": mult * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
@@ -616,8 +617,9 @@ def run_mixed(args):
                                       "(kernel_bench mixed --n 16384), scaled to this workload's launches")
     chain_flops = sum(2 * nb ** 3 / 3 + (n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_f32 (FP32 potrf + inverse of the 512x512 tile, one CTA) + "
-                          "k_colsolve_f32 (FP32 column solve)",
-                "bound": "latency (one CTA) / fp32-simt",
+                          + ("k_trsm2_bf16x3 (split-BF16 tcgen05 column solve)" if args.prec == "bf16x3"
+                             else "k_colsolve_f32 (FP32 column solve)"),
+                "bound": "latency (one CTA)",
                 "achieved": chain_flops / (fac_ms / 1e3) / 1e12 if fac_ms else None, "peak": None,
                 "unit": "TFLOP/s", "share_of_step": share_fac,
                 "note": "segments on two streams overlap the update; share is their summed device time"}

@@ -116,9 +116,11 @@ void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, cons
 int ooc_panel_plan(int64_t n, int nb, int64_t memBlock, int nx, int* out, int cap);
 
 /* ---- mixed precision: factor once, solve with FP64 iterative refinement -------- */
-/* Precision of the trailing syrk/gemm updates.  The diagonal-tile potrf and its inverse
- * always run in FP64; the column solve (a product with that inverse) runs in FP64 for
- * OOC_PREC_FP64 and in FP32 for the reduced-precision factors.                       */
+/* Precision of the trailing syrk/gemm updates.  OOC_PREC_FP64 factors the diagonal
+ * tiles (potrf and inverse) and solves the column panels in FP64.  The reduced-precision
+ * factors work in an FP32 matrix: FP32 diagonal tiles; the column solve (a product with
+ * the tile's inverse) in FP32 for OOC_PREC_FP32 and with the update's three BF16 tensor
+ * products for OOC_PREC_BF16X3 (nb a multiple of 128).                               */
 enum {
   OOC_PREC_FP64 = 0,  /* FP64 DMMA updates (the plain path)                        */
   OOC_PREC_FP32 = 1,  /* FP32 operands, FP32 FFMA accumulation                      */
