@@ -529,6 +529,9 @@ def run_mixed(args):
     torch.cuda.empty_cache()
 
     # ---- e2e: host A and b through the C-ABI ------------------------------------------
+    # The factor takes the pinned host matrix itself: it copies the lower triangle (the
+    # part a lower Cholesky reads) to the device once, keeps that FP64 copy for the
+    # refinement (OOC_OPT_KEEP_A), and the refinement given the same host pointer uses it.
     e2e = None
     if not args.skip_e2e:
         Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -536,22 +539,23 @@ def run_mixed(args):
         Bh = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
         Bh.copy_(B[:nrhs])
         Xh = torch.empty_like(Bh)
-        Ad = torch.empty_like(A)
         Bd = torch.empty((nrhs, n), dtype=torch.float64, device="cuda")
         Xd = torch.empty_like(Bd)
+        # host-to-device bytes of the lower triangle, column blocks as the library copies them
+        wblk = max(1, min(n, (256 << 20) // (8 * n)))
+        a_h2d = sum((n - c0) * min(wblk, n - c0) * 8 for c0 in range(0, n, wblk))
 
-        phase = {"h2d_ms": 0.0, "factor_ms": 0.0, "refine_ms": 0.0, "close_ms": 0.0, "d2h_ms": 0.0}
+        phase = {"h2d_b_ms": 0.0, "factor_incl_a_h2d_ms": 0.0, "refine_ms": 0.0, "close_ms": 0.0, "d2h_ms": 0.0}
 
         def e2e_step(record=False):
             t0 = time.perf_counter()
             with torch.cuda.stream(comp):
-                Ad.copy_(Ah, non_blocking=True)
                 Bd.copy_(Bh, non_blocking=True)
             comp.synchronize()
             t1 = time.perf_counter()
-            F = h.factor(Ad, n, n, nb, args.prec)
+            F = h.factor(Ah, n, n, nb, args.prec)
             t2 = time.perf_counter()
-            F.refine(Ad, n, Bd, n, Xd, n, nrhs, 1e-14, 30)
+            F.refine(Ah, n, Bd, n, Xd, n, nrhs, 1e-14, 30)
             t3 = time.perf_counter()
             F.close()
             t4 = time.perf_counter()
@@ -563,6 +567,7 @@ def run_mixed(args):
                 for k, v in zip(phase, (t1 - t0, t2 - t1, t3 - t2, t4 - t3, t5 - t4)):
                     phase[k] += v * 1e3 / args.steps
 
+        h.set_option(ooc.OPT_KEEP_A, 1)
         for _ in range(args.warmup):
             e2e_step()
         torch.cuda.synchronize()
@@ -574,10 +579,13 @@ def run_mixed(args):
         s1.record(comp)
         torch.cuda.synchronize()
         e_ms = allreduce_max(s0.elapsed_time(s1) / args.steps, world)
+        h.set_option(ooc.OPT_KEEP_A, 0)
         e2e = {"value": flops * world / (e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e_ms,
-               "h2d_bytes_per_step": int(n * n * 8 + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8),
+               "h2d_bytes_per_step": int(a_h2d + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8),
+               "path": "ooc_factor_create + ooc_solve_refine on the pinned host matrix (lower triangle copied "
+                       "once, kept for the refinement: OOC_OPT_KEEP_A)",
                "phases_ms_host_clock": {k: round(v, 2) for k, v in phase.items()}}
-        del Ah, Bh, Xh, Ad, Bd, Xd
+        del Ah, Bh, Xh, Bd, Xd
 
     # ---- roofline of the dominant kernel ------------------------------------------------
     # Trailing update of panel j (m = n - (j+1) nb rows below it, K = nb): algorithmic

@@ -57,8 +57,13 @@ enum {
   OOC_OPT_PROFILE = 3,     /* 1 = time kernels with CUDA events into ooc_stats       */
   OOC_OPT_PIN_HOST = 4,    /* 1 = page-lock a pageable host matrix for the call
                               (cudaHostRegister; default 1)                          */
-  OOC_OPT_REF_SCHEDULE = 5 /* 1 = panel widths exactly as oocdag.cpp:478-492 with one
+  OOC_OPT_REF_SCHEDULE = 5, /* 1 = panel widths exactly as oocdag.cpp:478-492 with one
                               X buffer counted (default 0: two X buffers counted)     */
+  OOC_OPT_KEEP_A = 6       /* 1 = a reduced-precision factor created from a HOST matrix
+                              keeps the FP64 lower triangle it copied to the device
+                              (8 n^2 more device bytes), and ooc_solve_refine given the
+                              same host pointer and lda uses it instead of copying A
+                              again (default 0)                                       */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */
@@ -142,9 +147,11 @@ int ooc_factor_copy_L(ooc_factor* F, double* L, int64_t ldl);
  * The dpotrs of the reference's VERIFY block (oocdag.cpp:439).                       */
 int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t ldb, int nrhs);
 /* Solve A X = B by iterative refinement: X0 from the factor, then R = B - A X in FP64
- * with the original A (device), correction with the factor (FP32 copy for a reduced-
- * precision factor), until the normwise backward error ||R||_inf/(||A||_inf ||X||_inf
- * + ||B||_inf) <= tol or maxiter corrections.  B, X: device, nrhs <= 16.             */
+ * with the original A, correction with the factor (FP32 copy for a reduced-precision
+ * factor), until the normwise backward error ||R||_inf/(||A||_inf ||X||_inf + ||B||_inf)
+ * <= tol or maxiter corrections.  A: device or host, lower triangle read (the residual
+ * and the norm use A's symmetry; a host A is copied to the device, lower triangle only,
+ * unless the factor kept it, OOC_OPT_KEEP_A).  B, X: device, nrhs <= 16.            */
 int ooc_solve_refine(ooc_handle* h, ooc_factor* F, const double* A, int64_t lda, const double* B,
                      int64_t ldb, double* X, int64_t ldx, int nrhs, double tol, int maxiter, int* iters,
                      double* berr);

@@ -34,6 +34,7 @@ OPT_TIMEOUT_MS = 2
 OPT_PROFILE = 3
 OPT_PIN_HOST = 4
 OPT_REF_SCHEDULE = 5
+OPT_KEEP_A = 6
 
 PREC_FP64 = 0
 PREC_FP32 = 1

@@ -822,27 +822,6 @@ __global__ void k_colmax_abs(const double* V, i64 ld, int n, int r, double* out 
   }
 }
 
-// Row sums of |A| (for ||A||_inf), one thread per row.
-// P[slice](row) = sum over the slice's columns of |A(row, c)| (stored FP64 A), for the
-// backward error's ||A||_inf: terms rounded to FP32 on the integer pipe and summed in FP32
-// over runs of 256 columns, the runs added in FP64 (relative error < 2e-5, which the
-// backward error's denominator does not notice; FP64 adds per element would cost ~2 ms
-// per 10^9 elements on this part).
-__global__ void __launch_bounds__(256) k_rowsum_abs(const double* __restrict__ A, i64 lda, i64 n, int kslice,
-                                                    double* __restrict__ P) {
-  const i64 row = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= n) return;
-  const i64 k0 = (i64)blockIdx.y * kslice;
-  const i64 k1 = min(k0 + kslice, n);
-  double s = 0;
-  for (i64 c0 = k0; c0 < k1; c0 += 256) {
-    const i64 c1 = min(k1, c0 + 256);
-    float f = 0.f;
-    for (i64 c = c0; c < c1; c++) f += fabsf(ooc_f64_to_f32(A[row + c * lda]));
-    s += ooc_f32_to_f64(f);
-  }
-  P[(i64)blockIdx.y * n + row] = s;
-}
 
 // R(:, q) -= A(seed) X(:, q) over the columns [blockIdx.y * kslice, ...) of A, with A
 // regenerated element by element (uniform generator) instead of read from memory.
@@ -1099,6 +1078,177 @@ int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
   return OOC_OK;
 }
 
+// ---- symmetric products reading only the lower triangle of A (FP64): the refinement's
+// residual Y = A X = tril(A) X + strict(A)^T X, and with ABS (|a|, X = ones when X is null)
+// the row sums of |A| for the infinity norm.  Nothing above the diagonal is loaded, so the
+// strict upper triangle may hold anything.
+//   k_symv_rows: CTA = 32 rows x a column slice (j <= i), warp w sums its eighth of each
+//                chunk; one partial sum per slice (as k_gemm_nn_small).
+//   k_symv_cols: one warp per column j, the dot products of A(j+1:n, j) with the rows of X
+//                (lane order, then a fixed shuffle tree).
+// The partial sums are added in slice order by k_symv_combine: the result is deterministic.
+template <bool ABS>
+__device__ __forceinline__ double symv_elem(double a) {
+  return ABS ? fabs(a) : a;
+}
+
+template <bool ABS, int R>
+__global__ void __launch_bounds__(256) k_symv_rows(const double* __restrict__ A, i64 lda,
+                                                   const double* __restrict__ X, i64 ldx, int n, int r, int kslice,
+                                                   double* __restrict__ P) {
+  __shared__ double Xs[R * NN_KCHUNK];  // q-major chunk of X; also the 8 x 32 x R partial sums
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = blockIdx.x * 32;
+  const int row = i0 + lane;
+  const int k0 = blockIdx.y * kslice;
+  const int k1 = min(min(n, k0 + kslice), i0 + 32);  // columns j <= the block's last row
+  double acc[R];
+#pragma unroll
+  for (int q = 0; q < R; q++) acc[q] = 0;
+  const double* Arow = A + (row < n ? row : 0);
+  for (int kc = k0; kc < k1; kc += NN_KCHUNK) {
+    const int kn = min(NN_KCHUNK, k1 - kc);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
+      const int q = idx / kn, kk = idx % kn;
+      Xs[q * NN_KCHUNK + kk] = (q < r) ? (X ? X[(kc + kk) + (i64)q * ldx] : 1.0) : 0.0;
+    }
+    __syncthreads();
+    const int kw = (kn + 7) / 8;
+    const int ka = warp * kw, kb = min(kn, ka + kw);
+    if (row < n) {
+      int kk = ka;
+      for (; kk + 8 <= kb; kk += 8) {
+        double a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int j = kc + kk + u;
+          a[u] = (j <= row) ? symv_elem<ABS>(Arow[(i64)j * lda]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Xs[q * NN_KCHUNK + kk + u], acc[q]);
+      }
+      for (; kk < kb; kk++) {
+        const int j = kc + kk;
+        const double a = (j <= row) ? symv_elem<ABS>(Arow[(i64)j * lda]) : 0.0;
+#pragma unroll
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Xs[q * NN_KCHUNK + kk], acc[q]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < R; q++) Xs[(warp * 32 + lane) * R + q] = acc[q];
+  __syncthreads();
+  if (warp != 0 || row >= n) return;
+  double* Pz = P + (i64)blockIdx.y * n * r;
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    if (q >= r) break;
+    double v = Xs[lane * R + q];
+#pragma unroll
+    for (int w = 1; w < 8; w++) v += Xs[(w * 32 + lane) * R + q];
+    Pz[row + (i64)q * n] = v;
+  }
+}
+
+template <bool ABS, int R>
+__global__ void __launch_bounds__(256) k_symv_cols(const double* __restrict__ A, i64 lda,
+                                                   const double* __restrict__ X, i64 ldx, int n, int r,
+                                                   double* __restrict__ Q) {
+  __shared__ double Xs[R * NN_KCHUNK];  // q-major chunk of X rows
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int jmin = blockIdx.x * 8;
+  const int j = jmin + warp;
+  double acc[R];
+#pragma unroll
+  for (int q = 0; q < R; q++) acc[q] = 0;
+  const double* Acol = A + (i64)(j < n ? j : 0) * lda;
+  for (int ic = jmin + 1; ic < n; ic += NN_KCHUNK) {
+    const int kn = min(NN_KCHUNK, n - ic);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
+      const int q = idx / kn, ii = idx % kn;
+      Xs[q * NN_KCHUNK + ii] = (q < r) ? (X ? X[(ic + ii) + (i64)q * ldx] : 1.0) : 0.0;
+    }
+    __syncthreads();
+    if (j < n) {
+      int ii = lane;
+      for (; ii + 96 < kn; ii += 128) {
+        double a[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = ic + ii + 32 * u;
+          a[u] = (i > j) ? symv_elem<ABS>(Acol[i]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Xs[q * NN_KCHUNK + ii + 32 * u], acc[q]);
+      }
+      for (; ii < kn; ii += 32) {
+        const int i = ic + ii;
+        const double a = (i > j) ? symv_elem<ABS>(Acol[i]) : 0.0;
+#pragma unroll
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Xs[q * NN_KCHUNK + ii], acc[q]);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    double v = acc[q];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    acc[q] = v;
+  }
+  if (j >= n || lane != 0) return;
+#pragma unroll
+  for (int q = 0; q < R; q++)
+    if (q < r) Q[j + (i64)q * n] = acc[q];
+}
+
+// C = beta C + alpha (sum of the nslice partials in order + Q)
+__global__ void k_symv_combine(const double* __restrict__ P, int nslice, const double* __restrict__ Q, double* C,
+                               i64 ldc, int n, int r, double alpha, double beta) {
+  const i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < r; q++) {
+    double v = 0;
+    for (int z = 0; z < nslice; z++) v += P[(i64)z * n * r + i + (i64)q * n];
+    v += Q[i + (i64)q * n];
+    double* c = C + i + (i64)q * ldc;
+    *c = (beta != 0.0) ? fma(alpha, v, beta * *c) : alpha * v;
+  }
+}
+
+// C (n x r, ld ldc) = beta C + alpha A X with A symmetric, given by its lower triangle
+// (ld lda).  abs: |A| instead of A; X null: a column of ones (r = 1).
+int symv_lower(bool abs, const double* A, i64 lda, const double* X, i64 ldx, double* C, i64 ldc, int n, int r,
+               double alpha, double beta, cudaStream_t s, DevBuf& part) {
+  if (n <= 0 || r <= 0) return OOC_OK;
+  if (r > RMAX || (!X && r != 1)) return OOC_ERR_UNSUPPORTED;
+  int nslice = (n + 2047) / 2048;
+  const int kslice = ((n + nslice - 1) / nslice + NN_KCHUNK - 1) / NN_KCHUNK * NN_KCHUNK;
+  nslice = (n + kslice - 1) / kslice;
+  int rc = part.ensure((size_t)(nslice + 1) * n * r * sizeof(double));
+  if (rc) return rc;
+  double* P = (double*)part.p;
+  double* Q = P + (size_t)nslice * n * r;
+  const dim3 grow((unsigned)((n + 31) / 32), (unsigned)nslice);
+  const unsigned gcol = (unsigned)((n + 7) / 8);
+  if (abs) {
+    k_symv_rows<true, 1><<<grow, 256, 0, s>>>(A, lda, X, ldx, n, r, kslice, P);
+    k_symv_cols<true, 1><<<gcol, 256, 0, s>>>(A, lda, X, ldx, n, r, Q);
+  } else {
+    NN_DISPATCH(r, (k_symv_rows<false, RR><<<grow, 256, 0, s>>>(A, lda, X, ldx, n, r, kslice, P)));
+    NN_DISPATCH(r, (k_symv_cols<false, RR><<<gcol, 256, 0, s>>>(A, lda, X, ldx, n, r, Q)));
+  }
+  k_symv_combine<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, nslice, Q, C, ldc, n, r, alpha, beta);
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
 // Solve L L^T X = B in place (B: n x r, ld ldb) using the inverses of the diagonal
 // tiles.  Dinv_J holds L_JJ^{-T} (column-major, upper), i.e. the transpose of
 // L_JJ^{-1}; tmp holds nb x r.
@@ -1172,7 +1322,13 @@ struct ooc_factor {
   int info = 0;
   DevBuf part, partf, work, scratch;
   DevBuf work2;  // BF16 planes of the panel before its tensor-core column solve
+  // FP64 copy of a host A's lower triangle (ld n), kept for the refinement
+  // (OOC_OPT_KEEP_A); A64_src / A64_lda identify the host matrix it came from.
+  double* A64 = nullptr;
+  const double* A64_src = nullptr;
+  i64 A64_lda = 0;
   ~ooc_factor() {
+    if (A64) cudaFree(A64);
     if (L) cudaFree(L);
     if (Dinv) cudaFree(Dinv);
     if (Lf && owns_Lf) cudaFree(Lf);
@@ -1469,19 +1625,34 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
       if (on_device) {
         k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256, 0, s>>>(A, lda, F->Lf, n, n,
                                                                                              0, (int)n, 0);
-      } else {  // host matrix: column blocks through a staging buffer
+      } else {  // host matrix: the lower part of each column block (rows c0..n-1), either
+                // into the kept FP64 copy (OOC_OPT_KEEP_A) or through a staging buffer
+        int64_t keep = 0;
+        ooc_get_option(h, OOC_OPT_KEEP_A, &keep);
         const int w = (int)std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
         DevBuf stage;
-        rc = stage.ensure((size_t)n * w * sizeof(double));
+        if (keep) {
+          if (cudaMalloc(&F->A64, (size_t)n * n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            F->A64 = nullptr;
+            rc = OOC_ERR_NOMEM;
+          } else {
+            F->A64_src = A;
+            F->A64_lda = lda;
+          }
+        } else {
+          rc = stage.ensure((size_t)n * w * sizeof(double));
+        }
         for (i64 c0 = 0; !rc && c0 < n; c0 += w) {
           const int wc = (int)std::min<i64>(w, n - c0);
-          if (cudaMemcpy2DAsync(stage.p, n * sizeof(double), A + c0 * lda, lda * sizeof(double), n * sizeof(double), wc,
-                                cudaMemcpyHostToDevice, s) != cudaSuccess) {
+          double* dst = keep ? F->A64 + c0 * n : (double*)stage.p;  // column c0 of the block, ld n
+          if (cudaMemcpy2DAsync(dst + c0, n * sizeof(double), A + c0 + c0 * lda, lda * sizeof(double),
+                                (n - c0) * sizeof(double), wc, cudaMemcpyHostToDevice, s) != cudaSuccess) {
             rc = OOC_ERR_CUDA;
             break;
           }
           k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min(wc, 1024)), 256, 0, s>>>(
-              (const double*)stage.p, n, F->Lf + c0 * n, n, n, c0, wc, 0);
+              dst, n, F->Lf + c0 * n, n, n, c0, wc, 0);
         }
         if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = OOC_ERR_CUDA;  // before the staging buffer goes
       }
@@ -1694,6 +1865,34 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     return OOC_ERR_NOMEM;
   }
   int rc = OOC_OK;
+  // A given on the host: the lower triangle the factor kept (same pointer and lda), else
+  // a device copy of the lower triangle, column block by column block.
+  double* Atmp = nullptr;
+  if (!gen) {
+    cudaPointerAttributes pa{};
+    const bool on_device = cudaPointerGetAttributes(&pa, Astore) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+    cudaGetLastError();
+    if (!on_device) {
+      if (F->A64 && Astore == F->A64_src && lda == F->A64_lda) {
+        Astore = F->A64;
+        lda = n;
+      } else if (cudaMalloc(&Atmp, (size_t)n * n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        Atmp = nullptr;
+        rc = OOC_ERR_NOMEM;
+      } else {
+        const i64 w = std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
+        for (i64 c0 = 0; !rc && c0 < n; c0 += w) {
+          const i64 wc = std::min<i64>(w, n - c0);
+          if (cudaMemcpy2DAsync(Atmp + c0 + c0 * n, n * sizeof(double), Astore + c0 + c0 * lda, lda * sizeof(double),
+                                (n - c0) * sizeof(double), wc, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            rc = OOC_ERR_CUDA;
+        }
+        Astore = Atmp;
+        lda = n;
+      }
+    }
+  }
   std::vector<double> hv((size_t)nred * r);
   const unsigned gb = (unsigned)((n + 255) / 256);
   // column slices of the generated products (enough CTAs to fill the GPU)
@@ -1744,12 +1943,8 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
         k_rowsum_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, gks, (double*)F->part.p);
         k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
       }
-    } else {
-      rc = F->part.ensure((size_t)gslices * n * sizeof(double));
-      if (!rc) {
-        k_rowsum_abs<<<dim3(gb, gslices), 256, 0, s>>>(Astore, lda, n, gks, (double*)F->part.p);
-        k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
-      }
+    } else if (!rc) {  // |A| 1 from the lower triangle
+      rc = symv_lower(true, Astore, lda, nullptr, 0, rows, n, (int)n, 1, 1.0, 0.0, s, F->part);
     }
     std::vector<double> nv;
     if (!rc) rc = colmax(rows, n, 1, nv);
@@ -1780,7 +1975,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
       cudaError_t e = cudaGetLastError();
       if (e != cudaSuccess) { ooc_set_last_error(e, "generated residual", __FILE__, __LINE__); rc = OOC_ERR_CUDA; break; }
     } else {
-      rc = gemm_nn_small<double, double>(Astore, lda, X, ldx, R, n, (int)n, (int)n, r, -1.0, 1.0, s, &F->part);
+      rc = symv_lower(false, Astore, lda, X, ldx, R, n, (int)n, r, -1.0, 1.0, s, F->part);
       if (rc) break;
     }
     rc = colmax(R, n, r, nr);
@@ -1807,6 +2002,10 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   }
   if (!rc) rc = ooc_wait_stream(h, s);
   if (solve_graph) cudaGraphExecDestroy(solve_graph);
+  if (Atmp) {
+    cudaStreamSynchronize(s);
+    cudaFree(Atmp);
+  }
   cudaFree(R);
   cudaFree(red);
   cudaFree(rows);

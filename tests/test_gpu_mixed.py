@@ -195,3 +195,34 @@ def test_reduced_factor_keeps_only_fp32(oracle_mod, handle, ooc):
     Lo = A.copy(order="F")
     oracle_mod.cholesky(Lo, nb, 1 << 30, 4, 2)
     assert np.abs(low - np.tril(Lo)).max() <= 1e-3 * np.abs(np.tril(Lo)).max()
+
+
+@pytest.mark.parametrize("where,keep", [("host", 1), ("host", 0), ("device", 0)])
+def test_refine_reads_only_the_lower_triangle(oracle_mod, handle, ooc, where, keep):
+    # The factor and the refinement read only A's lower triangle (the residual and the
+    # norm use A's symmetry): NaN above the diagonal must not reach the solution.  A host
+    # A is copied once, lower triangle only; with OOC_OPT_KEEP_A the refinement reuses the
+    # factor's device copy instead of copying it again.
+    import torch
+
+    n, nb, r = 1100, 256, 3
+    A, _ = _c2_matrix(oracle_mod, n, 0.1)
+    An = A.copy(order="F")
+    An[np.triu_indices(n, 1)] = np.nan
+    B = np.asfortranarray(np.random.default_rng(2).standard_normal((n, r)))
+    if where == "host":
+        Ain = torch.from_numpy(np.ascontiguousarray(An.T)).pin_memory()  # column-major storage
+    else:
+        Ain = _dev(An)
+    Bd, Xd = _dev(B), _dev(np.zeros((n, r)))
+    handle.set_option(ooc.OPT_KEEP_A, keep)
+    try:
+        with handle.factor(Ain, n, n, nb, "bf16x3") as F:
+            assert F.info == 0
+            it, be = F.refine(Ain, n, Bd, n, Xd, n, r, BERR_TOL, 30)
+    finally:
+        handle.set_option(ooc.OPT_KEEP_A, 0)
+    assert be <= BERR_TOL and it <= 5
+    X = _host(Xd)
+    assert np.isfinite(X).all()
+    assert _berr(A, X, B) <= 2 * BERR_TOL
