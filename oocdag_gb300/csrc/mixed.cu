@@ -710,8 +710,8 @@ __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A,
     __syncthreads();
     for (int idx = threadIdx.x; idx < kn * R; idx += blockDim.x) {
       const int q = idx / kn, kk = idx % kn;
-      Bs[kk * R + q] = (q < r) ? B[(kc + kk) + (i64)q * ldb] : TC(0);
-    }
+      Bs[q * NN_KCHUNK + kk] = (q < r) ? B[(kc + kk) + (i64)q * ldb] : TC(0);  // q-major: lanes read
+    }                                                                         // consecutive kk
     __syncthreads();
     if (row < m) {
       int kk = lane;
@@ -722,12 +722,12 @@ __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A,
 #pragma unroll
         for (int u = 0; u < 4; u++)
 #pragma unroll
-          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[(kk + 32 * u) * R + q], acc[q]);
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[q * NN_KCHUNK + kk + 32 * u], acc[q]);
       }
       for (; kk < kn; kk += 32) {
         const TC a = (TC)Acol[kc + kk];
 #pragma unroll
-        for (int q = 0; q < R; q++) acc[q] = fma(a, Bs[kk * R + q], acc[q]);
+        for (int q = 0; q < R; q++) acc[q] = fma(a, Bs[q * NN_KCHUNK + kk], acc[q]);
       }
     }
   }
@@ -1079,8 +1079,11 @@ int gemm_tn_small(const TA* A, i64 lda, const TC* B, i64 ldb, TC* C, i64 ldc, in
 }
 
 // ---- symmetric products reading only the lower triangle of A (FP64): the refinement's
-// residual Y = A X = tril(A) X + strict(A)^T X, and with ABS (|a|, X = ones when X is null)
-// the row sums of |A| for the infinity norm.  Nothing above the diagonal is loaded, so the
+// residual Y = A X = tril(A) X + strict(A)^T X, and with ABS the row sums of |A| for the
+// infinity norm (X null, r = 1): |a| rounded to FP32 on the integer pipe and summed in FP32
+// over runs of at most 32 elements, the runs added in FP64 (relative error < 1e-5, which the
+// backward error's denominator does not notice; an FP64 operation per element would cost
+// ~2 ms per 10^9 elements on this part).  Nothing above the diagonal is loaded, so the
 // strict upper triangle may hold anything.
 //   k_symv_rows: CTA = 32 rows x a column slice (j <= i), warp w sums its eighth of each
 //                chunk; one partial sum per slice (as k_gemm_nn_small).
@@ -1116,7 +1119,20 @@ __global__ void __launch_bounds__(256) k_symv_rows(const double* __restrict__ A,
     __syncthreads();
     const int kw = (kn + 7) / 8;
     const int ka = warp * kw, kb = min(kn, ka + kw);
-    if (row < n) {
+    if (ABS && row < n) {  // |a| rounded to FP32 (integer pipe), FP32 run of <= 32 per chunk
+      float f = 0.f;
+      int kk = ka;
+      for (; kk + 8 <= kb; kk += 8) {
+        double a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] = (kc + kk + u <= row) ? Arow[(i64)(kc + kk + u) * lda] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 8; u++) f += fabsf(ooc_f64_to_f32(a[u]));
+      }
+      for (; kk < kb; kk++)
+        if (kc + kk <= row) f += fabsf(ooc_f64_to_f32(Arow[(i64)(kc + kk) * lda]));
+      acc[0] += ooc_f32_to_f64(f);
+    } else if (row < n) {
       int kk = ka;
       for (; kk + 8 <= kb; kk += 8) {
         double a[8];
@@ -1174,7 +1190,20 @@ __global__ void __launch_bounds__(256) k_symv_cols(const double* __restrict__ A,
       Xs[q * NN_KCHUNK + ii] = (q < r) ? (X ? X[(ic + ii) + (i64)q * ldx] : 1.0) : 0.0;
     }
     __syncthreads();
-    if (j < n) {
+    if (ABS && j < n) {  // |a| rounded to FP32, FP32 run of <= 8 per chunk
+      float f = 0.f;
+      int ii = lane;
+      for (; ii + 96 < kn; ii += 128) {
+        double a[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) a[u] = (ic + ii + 32 * u > j) ? Acol[ic + ii + 32 * u] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) f += fabsf(ooc_f64_to_f32(a[u]));
+      }
+      for (; ii < kn; ii += 32)
+        if (ic + ii > j) f += fabsf(ooc_f64_to_f32(Acol[ic + ii]));
+      acc[0] += ooc_f32_to_f64(f);
+    } else if (j < n) {
       int ii = lane;
       for (; ii + 96 < kn; ii += 128) {
         double a[4];
