@@ -59,11 +59,16 @@ enum {
                               (cudaHostRegister; default 1)                          */
   OOC_OPT_REF_SCHEDULE = 5, /* 1 = panel widths exactly as oocdag.cpp:478-492 with one
                               X buffer counted (default 0: two X buffers counted)     */
-  OOC_OPT_KEEP_A = 6       /* 1 = a reduced-precision factor created from a HOST matrix
+  OOC_OPT_KEEP_A = 6,      /* 1 = a reduced-precision factor created from a HOST matrix
                               keeps the FP64 lower triangle it copied to the device
                               (8 n^2 more device bytes), and ooc_solve_refine given the
                               same host pointer and lda uses it instead of copying A
                               again (default 0)                                       */
+  OOC_OPT_TAIL_ORDER = 7   /* split-BF16 factors with nb a multiple of 256: the last
+                              panels, from the first multiple of nb at or after order
+                              n - value, are nb/2 wide (their one-CTA diagonal tiles are
+                              ~3x cheaper where the trailing update no longer hides
+                              them); 0 = uniform nb-wide panels.  Default 24576.      */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */

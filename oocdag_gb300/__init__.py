@@ -35,6 +35,7 @@ OPT_PROFILE = 3
 OPT_PIN_HOST = 4
 OPT_REF_SCHEDULE = 5
 OPT_KEEP_A = 6
+OPT_TAIL_ORDER = 7
 
 PREC_FP64 = 0
 PREC_FP32 = 1

@@ -921,8 +921,8 @@ int launch_syrk_bf16x3_f32(const float* X, i64 ldx, float* C, i64 ldc, int m, in
                            int reserve_sms);
 size_t bf16x3_work_bytes(int m, int K);
 int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, size_t work_bytes, cudaStream_t s);
-int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xplanes, float* P, i64 ldp, int m, int K,
-                           void* swork, size_t sbytes, const int* status, cudaStream_t s);
+int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
+                           int K, void* swork, size_t sbytes, const int* status, cudaStream_t s);
 
 namespace {
 
@@ -1278,47 +1278,78 @@ int symv_lower(bool abs, const double* A, i64 lda, const double* X, i64 ldx, dou
   return OOC_OK;
 }
 
+// Panel schedule of a reduced-precision factor: nb-wide panels up to column tail0 (a
+// multiple of nb), then nb2-wide panels (tail0 = n: uniform nb).  Panel p starts at J0,
+// is LN wide, and its diagonal tile's inverse sits at Dinv + off with leading dimension ld
+// (the panel's nominal width): the tiles are stored one after the other.
+struct Panels {
+  i64 n = 0, tail0 = 0;
+  int nb = 0, nb2 = 0;
+  int count() const {
+    if (tail0 >= n) return (int)((n + nb - 1) / nb);
+    return (int)(tail0 / nb + (n - tail0 + nb2 - 1) / nb2);
+  }
+  void get(int p, i64* J0, int* LN, i64* off, int* ld) const {
+    const int hc = tail0 >= n ? count() : (int)(tail0 / nb);
+    if (p < hc) {
+      *J0 = (i64)p * nb;
+      *LN = (int)std::min<i64>(nb, n - *J0);
+      *off = (i64)p * nb * nb;
+      *ld = nb;
+    } else {
+      const int t = p - hc;
+      *J0 = tail0 + (i64)t * nb2;
+      *LN = (int)std::min<i64>(nb2, n - *J0);
+      *off = (i64)hc * nb * nb + (i64)t * nb2 * nb2;
+      *ld = nb2;
+    }
+  }
+};
+
 // Solve L L^T X = B in place (B: n x r, ld ldb) using the inverses of the diagonal
 // tiles.  Dinv_J holds L_JJ^{-T} (column-major, upper), i.e. the transpose of
-// L_JJ^{-1}; tmp holds nb x r.
+// L_JJ^{-1}; tmp holds nb x r (nb = the widest panel).
 // B := (L L^T)^{-1} B with the factor's L and kept diagonal inverses (r <= 16 columns):
 // the dpotrs of the reference's VERIFY block (oocdag.cpp:439).  Two launches per block
 // step: the product with the block's inverse into tmp, then the panel product, whose
 // first CTA also moves tmp into place.
 template <typename T>
-int solve_with(const T* L, i64 ldl, const T* Dinv, i64 n, int nb, T* B, i64 ldb, int r, T* tmp, cudaStream_t s,
+int solve_with(const T* L, i64 ldl, const T* Dinv, const Panels& P, T* B, i64 ldb, int r, T* tmp, cudaStream_t s,
                DevBuf* part) {
-  const int bb = (int)((n + nb - 1) / nb);
-  const i64 tile = (i64)nb * nb;
+  const i64 n = P.n;
+  const int nt = P.nb;  // ld of tmp
+  const int bb = P.count();
   int rc;
   // forward: L y = b
   for (int J = 0; J < bb; J++) {
-    const i64 J0 = (i64)J * nb;
-    const int LN = (int)std::min<i64>(nb, n - J0);
-    rc = gemm_tn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s);  // Dinv_J^T b_J
+    i64 J0, off;
+    int LN, ld;
+    P.get(J, &J0, &LN, &off, &ld);
+    rc = gemm_tn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s);  // Dinv_J^T b_J
     if (rc) return rc;
     const i64 rows = n - J0 - LN;
     if (rows > 0) {
-      rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, tmp, nb, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
-                               T(1), s, part, CopyOut<T>{tmp, nb, B + J0, ldb, LN});
+      rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, tmp, nt, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
+                               T(1), s, part, CopyOut<T>{tmp, nt, B + J0, ldb, LN});
       if (rc) return rc;
     } else {
-      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nt * sizeof(T), LN * sizeof(T), r,
                                      cudaMemcpyDeviceToDevice, s));
     }
   }
   // backward: L^T x = y
   for (int J = bb - 1; J >= 0; J--) {
-    const i64 J0 = (i64)J * nb;
-    const int LN = (int)std::min<i64>(nb, n - J0);
-    rc = gemm_nn_small<T, T>(Dinv + J * tile, nb, B + J0, ldb, tmp, nb, LN, LN, r, T(1), T(0), s, nullptr);
+    i64 J0, off;
+    int LN, ld;
+    P.get(J, &J0, &LN, &off, &ld);
+    rc = gemm_nn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s, nullptr);
     if (rc) return rc;
     if (J0 > 0) {  // y_{<J} -= L_{J,<J}^T x_J
-      rc = gemm_tn_small<T, T>(L + J0, ldl, tmp, nb, B, ldb, (int)J0, LN, r, T(-1), T(1), s,
-                               CopyOut<T>{tmp, nb, B + J0, ldb, LN});
+      rc = gemm_tn_small<T, T>(L + J0, ldl, tmp, nt, B, ldb, (int)J0, LN, r, T(-1), T(1), s,
+                               CopyOut<T>{tmp, nt, B + J0, ldb, LN});
       if (rc) return rc;
     } else {
-      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nb * sizeof(T), LN * sizeof(T), r,
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(B + J0, ldb * sizeof(T), tmp, nt * sizeof(T), LN * sizeof(T), r,
                                      cudaMemcpyDeviceToDevice, s));
     }
   }
@@ -1345,6 +1376,17 @@ struct ooc_factor {
   i64 ld = 0;              // leading dimension of Lf (n for a factor object)
   bool owns_Lf = true;     // false when Lf is a caller's matrix (ooc_spotrf_L)
   float* Dinvf = nullptr;
+  // panel schedule (reduced precision): nb-wide panels up to column tail0, then nb2-wide
+  i64 tail0 = 0;
+  int nb2 = 0;
+  Panels panels() const {
+    Panels P;
+    P.n = n;
+    P.nb = nb;
+    P.tail0 = (Lf && tail0 < n) ? tail0 : n;
+    P.nb2 = nb2 > 0 ? nb2 : nb;
+    return P;
+  }
   double* tmp = nullptr;   // nb x 16
   float* tmpf = nullptr;
   int* status = nullptr;   // device status word of the factorization
@@ -1505,12 +1547,13 @@ constexpr int kChainSMs = 1;  // the diagonal kernel is one CTA
 int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
-  const int bb = (int)((n + nb - 1) / nb);
+  const Panels P = F->panels();
+  const int bb = P.count();
   float* A = F->Lf;
   const i64 lda = F->ld;
   const i64 tile = (i64)nb * nb;
   if (nb > DG_MAX) return OOC_ERR_UNSUPPORTED;
-  const bool split = (nb % 128 == 0);
+  const bool split = (nb % 128 == 0) && (P.nb2 % 128 == 0);
   const bool tc_solve = split && prec == OOC_PREC_BF16X3 && n > nb;
   int rc = F->scratch.ensure((size_t)tile * (sizeof(float) + (tc_solve ? 2 * sizeof(__nv_bfloat16) : 0)));
   if (rc) return rc;
@@ -1518,7 +1561,7 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
   __nv_bfloat16* Xh = tc_solve ? reinterpret_cast<__nv_bfloat16*>(Xr + tile) : nullptr;  // its hi, lo planes
   __nv_bfloat16* Xl = tc_solve ? Xh + tile : nullptr;
   if (tc_solve) {  // planes of the panel before (work2) and after (work) the solve
-    const size_t pb = bf16x3_work_bytes((int)(n - nb), nb);
+    const size_t pb = bf16x3_work_bytes((int)(n - std::min(nb, P.nb2)), nb);
     if ((rc = F->work.ensure(pb)) || (rc = F->work2.ensure(pb))) return rc;
   }
   OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
@@ -1529,19 +1572,29 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     cudaEvent_t a, b;
     ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
   } guard{evA, evP};
+  auto width = [&](int p) -> int {  // width of panel p (0 past the last)
+    if (p >= bb) return 0;
+    i64 J0, off;
+    int LN, ld;
+    P.get(p, &J0, &LN, &off, &ld);
+    return LN;
+  };
   OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the matrix was filled on s0
   if (tc_solve) {  // panel 0 below its diagonal tile, beside the first diagonal kernel
-    rc = launch_split_bf16_f32(A + nb, lda, (int)(n - nb), nb, F->work2.p, F->work2.bytes, s0);
+    const int w0 = width(0);
+    rc = launch_split_bf16_f32(A + w0, lda, (int)(n - w0), w0, F->work2.p, F->work2.bytes, s0);
     if (rc) return rc;
   }
   for (int j = 0; j < bb; j++) {
-    const i64 J0 = (i64)j * nb;
-    const int LN = (int)std::min<i64>(nb, n - J0);
+    i64 J0, off;
+    int LN, ldd;
+    P.get(j, &J0, &LN, &off, &ldd);
+    const int LNn = width(j + 1);              // the next panel's width
+    const int bjn = (LNn + 127) / 128;         // its 128-wide block columns in the trailing matrix
     float* Djj = A + J0 + J0 * lda;
     OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
     if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + (i64)j * tile, nb, Xr, Xh, Xl,
-                                               F->status);
+    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
     OOC_CUDA_TRY(cudaGetLastError());
     if (prof->on) prof->mark(s1);
     OOC_CUDA_TRY(cudaEventRecord(evP, s1));
@@ -1551,8 +1604,8 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
       float* Pn = Djj + LN;
       if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
       if (tc_solve) {
-        rc = launch_trsm_bf16x3_f32(F->work2.p, F->work2.bytes, Xh, Pn, lda, (int)m, LN, F->work.p, F->work.bytes,
-                                    F->status, s0);
+        rc = launch_trsm_bf16x3_f32(F->work2.p, F->work2.bytes, Xh, Xl, Pn, lda, (int)m, LN, F->work.p,
+                                    F->work.bytes, F->status, s0);
         if (rc) return rc;
       } else {
         k_colsolve_f32<<<(unsigned)((m + CS_ROWS - 1) / CS_ROWS), FTHR, 0, s0>>>(Pn, lda, Xr, LN, (int)m, LN,
@@ -1567,21 +1620,20 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
       }
       float* C = A + (J0 + LN) * (1 + lda);
       if (tc_solve) {  // the planes come from the solve
-        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 0, 0);
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, bjn, 0, 0);
         if (rc) return rc;
         OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-        // panel j+1 is final now: its planes (rows below its diagonal tile; it is nb wide
-        // whenever rows remain below it), then the bulk of the update
-        if (m - nb > 0) {
-          rc = launch_split_bf16_f32(C + nb, lda, (int)(m - nb), nb, F->work2.p, F->work2.bytes, s0);
+        // panel j+1 is final now: its planes (rows below its diagonal tile), then the bulk
+        if (m - LNn > 0) {
+          rc = launch_split_bf16_f32(C + LNn, lda, (int)(m - LNn), LNn, F->work2.p, F->work2.bytes, s0);
           if (rc) return rc;
         }
-        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, bjn, -1, 0, kChainSMs);
       } else if (split) {
-        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, nb / 128, 1, 0);
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, 0, bjn, 1, 0);
         if (rc) return rc;
         OOC_CUDA_TRY(cudaEventRecord(evA, s0));
-        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, nb / 128, -1, 0, kChainSMs);
+        rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work, bjn, -1, 0, kChainSMs);
       } else {
         rc = syrk_f32(prec, Pn, lda, C, lda, (int)m, LN, F->status, s0, F->work);
         if (rc) return rc;
@@ -1627,6 +1679,17 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   F->ld = n;
   F->nb = nb;
   F->prec = prec;
+  F->tail0 = n;
+  F->nb2 = nb;
+  if (prec == OOC_PREC_BF16X3 && nb % 256 == 0 && n > nb) {  // nb/2-wide tail panels
+    int64_t tail = 0;
+    ooc_get_option(h, OOC_OPT_TAIL_ORDER, &tail);
+    if (tail > 0) {
+      const i64 t0 = std::max<i64>(0, n - tail);
+      F->tail0 = std::min<i64>(n, (t0 + nb - 1) / nb * nb);
+      F->nb2 = nb / 2;
+    }
+  }
   int rc = alloc_factor(F, n, nb, reduced);
   if (rc) { delete F; return rc; }
   cudaEvent_t e0, e1;
@@ -1858,12 +1921,12 @@ extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t
     if (rc) return rc;
     const unsigned gb = (unsigned)((n + 255) / 256);
     k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, (float*)bf.p, n, (int)n, nrhs);
-    rc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, (float*)bf.p, n, nrhs, F->tmpf, s, &F->partf);
+    rc = solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), (float*)bf.p, n, nrhs, F->tmpf, s, &F->partf);
     if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>((const float*)bf.p, n, B, ldb, (int)n, nrhs);
     if (!rc) rc = ooc_wait_stream(h, s);  // before the staging buffer goes
     return rc;
   }
-  rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, B, ldb, nrhs, F->tmp, s, &F->part);
+  rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), B, ldb, nrhs, F->tmp, s, &F->part);
   if (rc) return rc;
   return ooc_wait_stream(h, s);
 }
@@ -1947,7 +2010,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
       if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         crc = OOC_ERR_CUDA;
       } else {
-        crc = solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, nullptr);
+        crc = solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), Rf, n, r, F->tmpf, s, nullptr);
         if (cudaStreamEndCapture(s, &g) != cudaSuccess) crc = OOC_ERR_CUDA;
       }
       if (!crc && cudaGraphInstantiate(&solve_graph, g, 0) != cudaSuccess) {
@@ -1961,7 +2024,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
       }
     }
     if (solve_graph) return cudaGraphLaunch(solve_graph, s) == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
-    return solve_with<float>(F->Lf, n, F->Dinvf, n, F->nb, Rf, n, r, F->tmpf, s, &F->partf);
+    return solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), Rf, n, r, F->tmpf, s, &F->partf);
   };
   // ||A||_inf
   double normA = 0;
@@ -1988,7 +2051,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   } else if (!rc) {
     OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
                                    cudaMemcpyDeviceToDevice, s));
-    rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, X, ldx, r, F->tmp, s, &F->part);
+    rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), X, ldx, r, F->tmp, s, &F->part);
   }
   int it = 0;
   double be = 0;
@@ -2023,7 +2086,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
       if (rc) break;
       k_add_f32_cols<<<gb, 256, 0, s>>>(X, ldx, Rf, n, (int)n, r);
     } else {
-      rc = solve_with<double>(F->L, n, F->Dinv, n, F->nb, R, n, r, F->tmp, s, &F->part);
+      rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), R, n, r, F->tmp, s, &F->part);
       if (rc) break;
       k_axpy_cols<<<gb, 256, 0, s>>>(X, ldx, R, n, (int)n, r);
     }

@@ -67,6 +67,7 @@ struct ooc_handle {
   int pin_host = 1;
   int ref_schedule = 0;
   int keep_a = 0;
+  int64_t tail_order = 24576;
   int last_info = 0;
   std::vector<cudaEvent_t> ev_pool;  // reusable timing-free events
   size_t ev_next = 0;
@@ -198,6 +199,10 @@ extern "C" int ooc_set_option(ooc_handle* h, int key, int64_t v) {
     case OOC_OPT_PIN_HOST: h->pin_host = v ? 1 : 0; return OOC_OK;
     case OOC_OPT_REF_SCHEDULE: h->ref_schedule = v ? 1 : 0; return OOC_OK;
     case OOC_OPT_KEEP_A: h->keep_a = v ? 1 : 0; return OOC_OK;
+    case OOC_OPT_TAIL_ORDER:
+      if (v < 0) return -3;
+      h->tail_order = v;
+      return OOC_OK;
     default: return -2;
   }
 }
@@ -212,6 +217,7 @@ extern "C" int ooc_get_option(ooc_handle* h, int key, int64_t* v) {
     case OOC_OPT_PIN_HOST: *v = h->pin_host; return OOC_OK;
     case OOC_OPT_REF_SCHEDULE: *v = h->ref_schedule; return OOC_OK;
     case OOC_OPT_KEEP_A: *v = h->keep_a; return OOC_OK;
+    case OOC_OPT_TAIL_ORDER: *v = h->tail_order; return OOC_OK;
     default: return -2;
   }
 }

@@ -1175,14 +1175,14 @@ int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, siz
 
 // Column solve of an FP32 panel on the tensor cores, P = U X^T (k_trsm2_bf16x3).  `uwork`
 // holds the planes of the panel before the solve (launch_split_bf16_f32, m x K) followed by
-// the 256 bytes of block tickets; `xplanes` the hi then lo planes of X = L_jj^{-1} (K x K,
-// row-major).  The result goes to P (ld ldp) and, split, to the planes at `swork` in the
+// the 256 bytes of block tickets; `xhi`, `xlo` the hi and lo planes of X = L_jj^{-1}
+// (K x K, row-major, ld K).  The result goes to P (ld ldp) and, split, to the planes at `swork` in the
 // layout launch_syrk_bf16x3_f32 reads with do_split = 0.  K must be a multiple of 128.
-int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xplanes, float* P, i64 ldp, int m, int K,
-                           void* swork, size_t sbytes, const int* status, cudaStream_t s) {
+int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
+                           int K, void* swork, size_t sbytes, const int* status, cudaStream_t s) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (K % TB != 0) return OOC_ERR_UNSUPPORTED;
-  if (!status || !uwork || !xplanes || !swork) return OOC_ERR_INTERNAL;
+  if (!status || !uwork || !xhi || !xlo || !swork) return OOC_ERR_INTERNAL;
   if (ubytes < bf16x3_work_bytes(m, K) || sbytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
   int rc = get_encode();
   if (rc) return rc;
@@ -1190,8 +1190,8 @@ int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xplanes, floa
   __nv_bfloat16* uh = (__nv_bfloat16*)uwork;
   __nv_bfloat16* ul = uh + (size_t)Mp * Kp;
   unsigned long long* tickets = reinterpret_cast<unsigned long long*>(ul + (size_t)Mp * Kp);
-  __nv_bfloat16* xh = (__nv_bfloat16*)const_cast<void*>(xplanes);
-  __nv_bfloat16* xl = xh + (size_t)K * K;
+  __nv_bfloat16* xh = (__nv_bfloat16*)const_cast<void*>(xhi);
+  __nv_bfloat16* xl = (__nv_bfloat16*)const_cast<void*>(xlo);
   __nv_bfloat16* sh = (__nv_bfloat16*)swork;
   __nv_bfloat16* sl = sh + (size_t)Mp * Kp;
   CUtensorMap mu_h, mu_l, mx_h, mx_l;

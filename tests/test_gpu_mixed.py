@@ -226,3 +226,29 @@ def test_refine_reads_only_the_lower_triangle(oracle_mod, handle, ooc, where, ke
     X = _host(Xd)
     assert np.isfinite(X).all()
     assert _berr(A, X, B) <= 2 * BERR_TOL
+
+
+@pytest.mark.parametrize("tail", [0, 600, 32768])
+def test_tail_panels_schedule(oracle_mod, handle, ooc, tail):
+    # Split-BF16 factors switch to nb/2-wide panels for the last `tail` orders (rounded to
+    # a multiple of nb): uniform (0), a switch at column 512 with a ragged last panel (600
+    # at n=1100, nb=256) and all panels narrow (32768).  The factor, the kept diagonal
+    # inverses and the solves follow the same schedule.
+    n, nb, r = 1100, 256, 2
+    A, _ = _c2_matrix(oracle_mod, n, 0.1)
+    B = np.asfortranarray(np.random.default_rng(5).standard_normal((n, r)))
+    Bd, Xd = _dev(B), _dev(np.zeros((n, r)))
+    handle.set_option(ooc.OPT_TAIL_ORDER, tail)
+    try:
+        with handle.factor(_dev(A), n, n, nb, "bf16x3") as F:
+            assert F.info == 0
+            L = np.asfortranarray(np.full((n, n), np.nan))
+            F.copy_L(L, n)
+            it, be = F.refine(_dev(A), n, Bd, n, Xd, n, r, BERR_TOL, 30)
+    finally:
+        handle.set_option(ooc.OPT_TAIL_ORDER, 24576)
+    Lo = A.copy(order="F")
+    oracle_mod.cholesky(Lo, nb, 1 << 30, 4, 2)
+    assert np.abs(np.tril(L) - np.tril(Lo)).max() <= 1e-3 * np.abs(np.tril(Lo)).max()
+    assert be <= BERR_TOL and it <= 5
+    assert _berr(A, _host(Xd), B) <= 2 * BERR_TOL
