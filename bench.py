@@ -45,7 +45,7 @@ METRIC = "Cholesky TFLOP/s (n^3/3 flops), mixed vs FP64 at backward err<=1e-14; 
 # 44.02 GFLOP; profiles/k_panel_update_fp64_n8192.md).  The kernel's traffic is the
 # operand and C tiles, which scale with the flops of a launch at fixed nb.
 UPDATE_DRAM_BYTES_PER_FLOP = 348.1e6 / 44.02e9
-UPDATE_TRAFFIC_RATIO = 988.1 / 976.0  # tcgen05 update: ncu DRAM bytes / algorithmic bytes
+UPDATE_TRAFFIC_RATIO = 967.5 / 976.3  # k_syrk2_bf16x3 bulk launch, n=16384: ncu DRAM bytes / algorithmic bytes
 
 
 def parse():
@@ -593,10 +593,13 @@ def run_mixed(args):
     # the FP32 lower triangle read and written (8 B per element), the FP32 panel read by the
     # split (4 B per element) and the two BF16 planes written and read once (8 B per element).
     upd_bytes = kern_bytes = 0.0
-    for j in range(n // nb - 1):
-        m = n - (j + 1) * nb
-        upd_bytes += m * (m + 1) / 2 * 8 + m * nb * (4 + 8)
-        kern_bytes += m * (m + 1) / 2 * 8 + m * nb * 4  # what the tcgen05 kernel itself moves
+    panels = panel_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER))
+    for J0, LN in panels:
+        m = n - J0 - LN
+        if m <= 0:
+            continue
+        upd_bytes += m * (m + 1) / 2 * 8 + m * LN * (4 + 8)
+        kern_bytes += m * (m + 1) / 2 * 8 + m * LN * 4  # what the tcgen05 kernel itself moves
     upd_bytes *= args.steps
     kern_bytes *= args.steps
     share_upd = upd_ms / (ms_local * args.steps)
@@ -619,11 +622,12 @@ def run_mixed(args):
         upd_roof["frac"] = upd_roof["achieved"] / upd_roof["peak"]
     if args.prec == "bf16x3" and upd_launch:
         # DRAM bytes per launch: the algorithmic kernel bytes scaled by the measured/algorithmic
-        # ratio of one ncu capture (bulk update at n=16384: 988.1 MB measured, 976 MB algorithmic)
+        # ratio of one ncu capture (bulk update at n=16384, m=15872, block columns 4..:
+        # 967.5 MB measured, 976.3 MB algorithmic)
         upd_roof["traffic"] = UPDATE_TRAFFIC_RATIO * kern_bytes / upd_launch
         upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk-update launch "
                                       "(kernel_bench mixed --n 16384), scaled to this workload's launches")
-    chain_flops = sum(2 * nb ** 3 / 3 + (n - (j + 1) * nb) * nb * nb for j in range(n // nb)) * args.steps
+    chain_flops = sum(2 * LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in panels) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_f32 (FP32 potrf + inverse of the 512x512 tile, one CTA) + "
                           + ("k_trsm2_bf16x3 (split-BF16 tcgen05 column solve)" if args.prec == "bf16x3"
                              else "k_colsolve_f32 (FP32 column solve)"),
@@ -690,6 +694,21 @@ def run_mixed(args):
 # ----------------------------------------------------------------------------------
 # configs[3]: batched small systems in one persistent launch
 # ----------------------------------------------------------------------------------
+def panel_schedule(n, nb, prec, tail_order):
+    """(J0, width) of the factor's panels, as the library schedules them: nb wide, and for
+    split-BF16 factors with nb a multiple of 256 nb/2 wide from the first multiple of nb at
+    or after order n - tail_order (OOC_OPT_TAIL_ORDER)."""
+    t0 = n
+    if prec == "bf16x3" and nb % 256 == 0 and n > nb and tail_order > 0:
+        t0 = min(n, (max(0, n - tail_order) + nb - 1) // nb * nb)
+    out = [(j * nb, min(nb, n - j * nb)) for j in range((t0 + nb - 1) // nb)]
+    J0 = t0
+    while J0 < n:
+        out.append((J0, min(nb // 2, n - J0)))
+        J0 += nb // 2
+    return out
+
+
 def bench_batched(h, args, count=20000, reps=3):
     """20000 SPD systems, n ~ U{16..512}, A = M M^T/n + I (M ~ N(0,1)), one N(0,1) RHS each,
     FP64 and FP32; tile widths from the autotuner; results compared per matrix with the
