@@ -64,11 +64,17 @@ enum {
                               (8 n^2 more device bytes), and ooc_solve_refine given the
                               same host pointer and lda uses it instead of copying A
                               again (default 0)                                       */
-  OOC_OPT_TAIL_ORDER = 7   /* split-BF16 factors with nb a multiple of 256: the last
+  OOC_OPT_TAIL_ORDER = 7,  /* split-BF16 factors with nb a multiple of 256: the last
                               panels, from the first multiple of nb at or after order
                               n - value, are nb/2 wide (their one-CTA diagonal tiles are
                               ~3x cheaper where the trailing update no longer hides
                               them); 0 = uniform nb-wide panels.  Default 24576.      */
+  OOC_OPT_POOL_BYTES = 8   /* device bytes the handle may keep cached from destroyed
+                              factor objects for reuse by later ones of the same sizes
+                              (freeing multi-GB buffers costs ~0.4 ms per GB and
+                              synchronises the device); released by ooc_destroy, or when
+                              an allocation fails.  Default 40 % of device memory, 0 =
+                              no caching.                                             */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */

@@ -36,6 +36,7 @@ OPT_PIN_HOST = 4
 OPT_REF_SCHEDULE = 5
 OPT_KEEP_A = 6
 OPT_TAIL_ORDER = 7
+OPT_POOL_BYTES = 8
 
 PREC_FP64 = 0
 PREC_FP32 = 1

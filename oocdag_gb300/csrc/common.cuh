@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <memory>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -89,6 +91,9 @@ cudaStream_t ooc_compute_stream(ooc_handle* h);
 int ooc_device(ooc_handle* h);
 int ooc_wait_stream(ooc_handle* h, cudaStream_t s);  // bounded by the handle's timeout
 ooc_handle* ooc_default_handle();
+// The handle's device-buffer cache (devpool.cuh), shared with the factor objects it creates.
+struct DevPool;
+std::shared_ptr<DevPool> ooc_handle_pool(ooc_handle* h);
 
 // Generators (matgen.cu): fill the block of global rows [r0, r0+m) and columns
 // [c0, c0+nc) of the n x n test matrix into the device buffer B (leading dimension ldb).

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "devpool.cuh"
 
 namespace {
 
@@ -926,19 +927,33 @@ int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const vo
 
 namespace {
 
+// Device scratch that grows on demand.  With a pool (a factor object's buffers), the
+// buffer comes from the handle's cache and returns to it on destruction; a buffer replaced
+// by a larger one is freed at once (work queued on it may still be pending).
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  ~DevBuf() { if (p) cudaFree(p); }
+  DevPool* pool = nullptr;
+  ~DevBuf() {
+    if (!p) return;
+    if (pool) pool->release(p);
+    else cudaFree(p);
+  }
   int ensure(size_t b) {
     if (bytes >= b) return OOC_OK;
-    if (p) cudaFree(p);
+    if (p) {
+      if (pool) pool->drop(p);
+      else cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
-    if (cudaMalloc(&p, b) != cudaSuccess) {
+    if (pool) {
+      p = pool->alloc(b);
+    } else if (cudaMalloc(&p, b) != cudaSuccess) {
       cudaGetLastError();
-      return OOC_ERR_NOMEM;
+      p = nullptr;
     }
+    if (!p) return OOC_ERR_NOMEM;
     bytes = b;
     return OOC_OK;
   }
@@ -1391,6 +1406,9 @@ struct ooc_factor {
   float* tmpf = nullptr;
   int* status = nullptr;   // device status word of the factorization
   int info = 0;
+  // the handle's device-buffer cache (null: plain cudaMalloc / cudaFree); declared before
+  // the DevBufs so that it outlives them
+  std::shared_ptr<DevPool> pool;
   DevBuf part, partf, work, scratch;
   DevBuf work2;  // BF16 planes of the panel before its tensor-core column solve
   // FP64 copy of a host A's lower triangle (ld n), kept for the refinement
@@ -1398,15 +1416,33 @@ struct ooc_factor {
   double* A64 = nullptr;
   const double* A64_src = nullptr;
   i64 A64_lda = 0;
+  // a device buffer of the factor, from the pool when there is one
+  template <typename T>
+  int alloc(T** p, size_t bytes) {
+    *p = nullptr;
+    if (pool) {
+      *p = (T*)pool->alloc(bytes);
+    } else if (cudaMalloc((void**)p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      *p = nullptr;
+    }
+    return *p ? OOC_OK : OOC_ERR_NOMEM;
+  }
+  void release(void* p) {
+    if (!p) return;
+    if (pool) pool->release(p);
+    else cudaFree(p);
+  }
+  // destroyed after its device work is done (ooc_factor_destroy synchronises the device)
   ~ooc_factor() {
-    if (A64) cudaFree(A64);
-    if (L) cudaFree(L);
-    if (Dinv) cudaFree(Dinv);
-    if (Lf && owns_Lf) cudaFree(Lf);
-    if (Dinvf) cudaFree(Dinvf);
-    if (tmp) cudaFree(tmp);
-    if (tmpf) cudaFree(tmpf);
-    if (status) cudaFree(status);
+    release(A64);
+    release(L);
+    release(Dinv);
+    if (owns_Lf) release(Lf);
+    release(Dinvf);
+    release(tmp);
+    release(tmpf);
+    release(status);
   }
 };
 
@@ -1415,20 +1451,13 @@ namespace {
 int alloc_factor(ooc_factor* F, i64 n, int nb, bool reduced) {
   const int bb = (int)((n + nb - 1) / nb);
   const size_t tiles = (size_t)bb * nb * nb;
-  bool ok = cudaMalloc(&F->status, sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&F->tmp, (size_t)nb * RMAX * sizeof(double)) == cudaSuccess;
+  bool ok = !F->alloc(&F->status, sizeof(int)) && !F->alloc(&F->tmp, (size_t)nb * RMAX * sizeof(double));
   if (ok && !reduced)
-    ok = cudaMalloc(&F->L, (size_t)n * n * sizeof(double)) == cudaSuccess &&
-         cudaMalloc(&F->Dinv, tiles * sizeof(double)) == cudaSuccess;
+    ok = !F->alloc(&F->L, (size_t)n * n * sizeof(double)) && !F->alloc(&F->Dinv, tiles * sizeof(double));
   if (ok && reduced)
-    ok = cudaMalloc(&F->Lf, (size_t)n * n * sizeof(float)) == cudaSuccess &&
-         cudaMalloc(&F->Dinvf, tiles * sizeof(float)) == cudaSuccess &&
-         cudaMalloc(&F->tmpf, (size_t)nb * RMAX * sizeof(float)) == cudaSuccess;
-  if (!ok) {
-    cudaGetLastError();
-    return OOC_ERR_NOMEM;
-  }
-  return OOC_OK;
+    ok = !F->alloc(&F->Lf, (size_t)n * n * sizeof(float)) && !F->alloc(&F->Dinvf, tiles * sizeof(float)) &&
+         !F->alloc(&F->tmpf, (size_t)nb * RMAX * sizeof(float));
+  return ok ? OOC_OK : OOC_ERR_NOMEM;
 }
 
 struct MixedProf {
@@ -1690,6 +1719,8 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
       F->nb2 = nb / 2;
     }
   }
+  F->pool = ooc_handle_pool(h);
+  for (DevBuf* b : {&F->part, &F->partf, &F->work, &F->scratch, &F->work2}) b->pool = F->pool.get();
   int rc = alloc_factor(F, n, nb, reduced);
   if (rc) { delete F; return rc; }
   cudaEvent_t e0, e1;
@@ -1724,9 +1755,7 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
         const int w = (int)std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
         DevBuf stage;
         if (keep) {
-          if (cudaMalloc(&F->A64, (size_t)n * n * sizeof(double)) != cudaSuccess) {
-            cudaGetLastError();
-            F->A64 = nullptr;
+          if (F->alloc(&F->A64, (size_t)n * n * sizeof(double))) {
             rc = OOC_ERR_NOMEM;
           } else {
             F->A64_src = A;
@@ -1968,9 +1997,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
       if (F->A64 && Astore == F->A64_src && lda == F->A64_lda) {
         Astore = F->A64;
         lda = n;
-      } else if (cudaMalloc(&Atmp, (size_t)n * n * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        Atmp = nullptr;
+      } else if (F->alloc(&Atmp, (size_t)n * n * sizeof(double))) {
         rc = OOC_ERR_NOMEM;
       } else {
         const i64 w = std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
@@ -2096,7 +2123,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   if (solve_graph) cudaGraphExecDestroy(solve_graph);
   if (Atmp) {
     cudaStreamSynchronize(s);
-    cudaFree(Atmp);
+    F->release(Atmp);
   }
   cudaFree(R);
   cudaFree(red);

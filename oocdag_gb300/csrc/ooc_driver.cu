@@ -32,9 +32,11 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <memory>
 #include <vector>
 
 #include "common.cuh"
+#include "devpool.cuh"
 
 // ---------------------------------------------------------------------------------
 // Error reporting
@@ -68,6 +70,7 @@ struct ooc_handle {
   int ref_schedule = 0;
   int keep_a = 0;
   int64_t tail_order = 24576;
+  std::shared_ptr<DevPool> pool;  // device buffers of the handle's factor objects
   int last_info = 0;
   std::vector<cudaEvent_t> ev_pool;  // reusable timing-free events
   size_t ev_next = 0;
@@ -159,9 +162,18 @@ extern "C" int ooc_create(ooc_handle** out, int device) {
     g_last_error = "handle creation failed";
     return OOC_ERR_CUDA;
   }
+  h->pool = std::make_shared<DevPool>();
+  h->pool->device = device;
+  {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    h->pool->cap = tot / 10 * 4;  // default: 40 % of the device memory may stay cached
+  }
   *out = h;
   return OOC_OK;
 }
+
+std::shared_ptr<DevPool> ooc_handle_pool(ooc_handle* h) { return h ? h->pool : nullptr; }
 
 extern "C" int ooc_destroy(ooc_handle* h) {
   if (!h) return OOC_OK;
@@ -203,6 +215,10 @@ extern "C" int ooc_set_option(ooc_handle* h, int key, int64_t v) {
       if (v < 0) return -3;
       h->tail_order = v;
       return OOC_OK;
+    case OOC_OPT_POOL_BYTES:
+      if (v < 0) return -3;
+      if (h->pool) h->pool->set_cap((size_t)v);
+      return OOC_OK;
     default: return -2;
   }
 }
@@ -218,6 +234,7 @@ extern "C" int ooc_get_option(ooc_handle* h, int key, int64_t* v) {
     case OOC_OPT_REF_SCHEDULE: *v = h->ref_schedule; return OOC_OK;
     case OOC_OPT_KEEP_A: *v = h->keep_a; return OOC_OK;
     case OOC_OPT_TAIL_ORDER: *v = h->tail_order; return OOC_OK;
+    case OOC_OPT_POOL_BYTES: *v = h->pool ? (int64_t)h->pool->cap : 0; return OOC_OK;
     default: return -2;
   }
 }

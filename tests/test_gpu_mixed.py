@@ -252,3 +252,31 @@ def test_tail_panels_schedule(oracle_mod, handle, ooc, tail):
     assert np.abs(np.tril(L) - np.tril(Lo)).max() <= 1e-3 * np.abs(np.tril(Lo)).max()
     assert be <= BERR_TOL and it <= 5
     assert _berr(A, _host(Xd), B) <= 2 * BERR_TOL
+
+
+def test_pooled_buffers_give_identical_factors(oracle_mod, handle, ooc):
+    # Factor objects take their device buffers from the handle's cache and return them
+    # when destroyed; a factor built in reused buffers is bit-identical to one built in
+    # fresh ones (OOC_OPT_POOL_BYTES = 0: no caching), and the cap can be read back.
+    n, nb = 1100, 256
+    A, _ = _c2_matrix(oracle_mod, n, 0.1)
+    Ad = _dev(A)
+
+    def factor_L():
+        with handle.factor(Ad, n, n, nb, "bf16x3") as F:
+            assert F.info == 0
+            L = np.asfortranarray(np.full((n, n), np.nan))
+            F.copy_L(L, n)
+        return L
+
+    cap = handle.get_option(ooc.OPT_POOL_BYTES)
+    assert cap > 0
+    first = factor_L()
+    again = [factor_L() for _ in range(2)]  # sizes repeat: buffers come from the cache
+    handle.set_option(ooc.OPT_POOL_BYTES, 0)
+    try:
+        fresh = factor_L()
+    finally:
+        handle.set_option(ooc.OPT_POOL_BYTES, cap)
+    for L in again + [fresh]:
+        np.testing.assert_array_equal(L, first)
