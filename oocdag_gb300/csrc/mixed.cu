@@ -1411,6 +1411,7 @@ struct ooc_factor {
   std::shared_ptr<DevPool> pool;
   DevBuf part, partf, work, scratch;
   DevBuf work2;  // BF16 planes of the panel before its tensor-core column solve
+  DevBuf part2;  // partial sums of the refinement's norm (second stream)
   // FP64 copy of a host A's lower triangle (ld n), kept for the refinement
   // (OOC_OPT_KEEP_A); A64_src / A64_lda identify the host matrix it came from.
   double* A64 = nullptr;
@@ -1720,7 +1721,7 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     }
   }
   F->pool = ooc_handle_pool(h);
-  for (DevBuf* b : {&F->part, &F->partf, &F->work, &F->scratch, &F->work2}) b->pool = F->pool.get();
+  for (DevBuf* b : {&F->part, &F->partf, &F->work, &F->scratch, &F->work2, &F->part2}) b->pool = F->pool.get();
   int rc = alloc_factor(F, n, nb, reduced);
   if (rc) { delete F; return rc; }
   cudaEvent_t e0, e1;
@@ -1976,7 +1977,7 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   float* Rf = nullptr;
   const int nred = 152;
   if (cudaMalloc(&R, (size_t)n * r * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&red, (size_t)nred * r * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&red, (size_t)nred * (r + 1) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&rows, (size_t)n * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&Rf, (size_t)n * r * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
@@ -2054,20 +2055,33 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     return solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), Rf, n, r, F->tmpf, s, &F->partf);
   };
   // ||A||_inf
+  // ||A||_inf on the handle's second stream, beside X0's solve (a chain of small launches
+  // that leaves most of the GPU idle): row sums into `rows`, their maximum per CTA into
+  // the last nred words of `red`, read once X0 has been issued.
   double normA = 0;
+  double* red_norm = red + (size_t)nred * r;
+  cudaStream_t s2 = s;
   {
+    void* p2 = nullptr;
+    if (ooc_get_stream(h, 1, &p2) == OOC_OK && p2) s2 = (cudaStream_t)p2;
+  }
+  cudaEvent_t ev_in = nullptr;
+  if (!rc && s2 != s) {
+    if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess || cudaEventRecord(ev_in, s) != cudaSuccess ||
+        cudaStreamWaitEvent(s2, ev_in, 0) != cudaSuccess)
+      rc = OOC_ERR_CUDA;
+  }
+  if (!rc) {
     if (gen) {
-      rc = F->part.ensure((size_t)gslices * n * sizeof(double));
+      rc = F->part2.ensure((size_t)gslices * n * sizeof(double));
       if (!rc) {
-        k_rowsum_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, gks, (double*)F->part.p);
-        k_sum_slices_rows<<<gb, 256, 0, s>>>((const double*)F->part.p, gslices, n, rows);
+        k_rowsum_gen<<<dim3(gb, gslices), 256, 0, s2>>>(key, n, alpha, gks, (double*)F->part2.p);
+        k_sum_slices_rows<<<gb, 256, 0, s2>>>((const double*)F->part2.p, gslices, n, rows);
       }
-    } else if (!rc) {  // |A| 1 from the lower triangle
-      rc = symv_lower(true, Astore, lda, nullptr, 0, rows, n, (int)n, 1, 1.0, 0.0, s, F->part);
+    } else {  // |A| 1 from the lower triangle
+      rc = symv_lower(true, Astore, lda, nullptr, 0, rows, n, (int)n, 1, 1.0, 0.0, s2, F->part2);
     }
-    std::vector<double> nv;
-    if (!rc) rc = colmax(rows, n, 1, nv);
-    if (!rc) normA = nv[0];
+    if (!rc) k_colmax_abs<<<nred, 256, 0, s2>>>(rows, n, (int)n, 1, red_norm);
   }
   std::vector<double> nb_(r), nx(r), nr(r);
   if (!rc) rc = colmax(B, ldb, r, nb_);
@@ -2079,6 +2093,13 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
                                    cudaMemcpyDeviceToDevice, s));
     rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), X, ldx, r, F->tmp, s, &F->part);
+  }
+  if (!rc) rc = ooc_wait_stream(h, s2);
+  if (!rc) {
+    std::vector<double> hn(nred);
+    if (cudaMemcpy(hn.data(), red_norm, (size_t)nred * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = OOC_ERR_CUDA;
+    for (int b = 0; !rc && b < nred; b++) normA = std::max(normA, hn[b]);
   }
   int it = 0;
   double be = 0;
@@ -2120,6 +2141,8 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     it++;
   }
   if (!rc) rc = ooc_wait_stream(h, s);
+  if (s2 != s) cudaStreamSynchronize(s2);  // the norm's buffers may go now
+  if (ev_in) cudaEventDestroy(ev_in);
   if (solve_graph) cudaGraphExecDestroy(solve_graph);
   if (Atmp) {
     cudaStreamSynchronize(s);
