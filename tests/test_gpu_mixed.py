@@ -228,13 +228,14 @@ def test_refine_reads_only_the_lower_triangle(oracle_mod, handle, ooc, where, ke
     assert _berr(A, X, B) <= 2 * BERR_TOL
 
 
-@pytest.mark.parametrize("tail", [0, 600, 32768])
-def test_tail_panels_schedule(oracle_mod, handle, ooc, tail):
+@pytest.mark.parametrize("nb,tail", [(256, 0), (256, 600), (256, 32768), (512, 600)])
+def test_tail_panels_schedule(oracle_mod, handle, ooc, nb, tail):
     # Split-BF16 factors switch to nb/2-wide panels for the last `tail` orders (rounded to
     # a multiple of nb): uniform (0), a switch at column 512 with a ragged last panel (600
     # at n=1100, nb=256) and all panels narrow (32768).  The factor, the kept diagonal
-    # inverses and the solves follow the same schedule.
-    n, nb, r = 1100, 256, 2
+    # inverses and the solves follow the same schedule; nb=512 with the switch at column 512
+    # mixes 512- and 256-wide diagonal tiles in one factorization.
+    n, r = 1100, 2
     A, _ = _c2_matrix(oracle_mod, n, 0.1)
     B = np.asfortranarray(np.random.default_rng(5).standard_normal((n, r)))
     Bd, Xd = _dev(B), _dev(np.zeros((n, r)))
