@@ -43,9 +43,11 @@ __device__ __forceinline__ T tsqrt(T x) { return sqrt(x); }
 template <>
 __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
 
-// Shared layout: D[64][65] (diagonal block), P[NMAX][blk+1] (panel copy).
-template <typename T>
-__device__ int factor_one(T* __restrict__ A, int n, int blk, T* D, T* P, int* s_fail) {
+// Shared layout: D[64][65] (diagonal block), P[NMAX][blk+1] (panel copy).  BLK is the
+// panel width (a compile-time constant, so that the panel solve keeps its row in registers).
+template <typename T, int BLK>
+__device__ int factor_one(T* __restrict__ A, int n, T* D, T* P, int* s_fail) {
+  constexpr int blk = BLK;
   const int t = threadIdx.x;
   const int ldp = blk + 1;
   for (int k = 0; k < n; k += blk) {
@@ -84,18 +86,28 @@ __device__ int factor_one(T* __restrict__ A, int n, int blk, T* D, T* P, int* s_
     if (fail) return fail;
     const int m = n - k - kb;
     if (m <= 0) break;
-    // 2. panel: rows below, B := B L_kk^-T, one thread per row; result kept in P
+    // 2. panel: rows below, B := B L_kk^-T, one thread per row held in registers (the
+    // dependent chain then waits on FMAs, not on shared-memory loads); result kept in P.
+    // Columns c >= kb are computed from stale D entries and discarded.
     for (int i = t; i < m; i += BT) {
-      T* row = P + i * ldp;
       const int gi = k + kb + i;
-      for (int c = 0; c < kb; c++) row[c] = A[gi + (i64)(k + c) * n];
-      for (int c = 0; c < kb; c++) {
-        T v = row[c];
-        for (int q = 0; q < c; q++) v -= row[q] * D[q * 65 + c];
-        v /= D[c * 65 + c];
-        row[c] = v;
-        A[gi + (i64)(k + c) * n] = v;
+      T r[BLK];
+#pragma unroll
+      for (int c = 0; c < BLK; c++) r[c] = (c < kb) ? A[gi + (i64)(k + c) * n] : T(0);
+#pragma unroll
+      for (int c = 0; c < BLK; c++) {
+        T v = r[c];
+#pragma unroll
+        for (int q = 0; q < c; q++) v -= r[q] * D[q * 65 + c];
+        r[c] = (c < kb) ? v / D[c * 65 + c] : T(0);
       }
+      T* row = P + i * ldp;
+#pragma unroll
+      for (int c = 0; c < BLK; c++)
+        if (c < kb) {
+          row[c] = r[c];
+          A[gi + (i64)(k + c) * n] = r[c];
+        }
     }
     __syncthreads();
     // 3. trailing update of the lower triangle from P (4 x 4 tiles per thread)
@@ -203,7 +215,15 @@ __global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ it
     if (idx >= count) break;
     const Item it = items[idx];
     T* a = (T*)it.a;
-    const int f = (it.mode == 0) ? factor_one<T>(a, it.n, it.blk, D, P, &s_fail) : 0;
+    int f = 0;
+    if (it.mode == 0) {
+      switch (it.blk) {  // the widths the autotuner chooses from (others fall back to 32)
+        case 8: f = factor_one<T, 8>(a, it.n, D, P, &s_fail); break;
+        case 16: f = factor_one<T, 16>(a, it.n, D, P, &s_fail); break;
+        case 64: f = factor_one<T, 64>(a, it.n, D, P, &s_fail); break;
+        default: f = factor_one<T, 32>(a, it.n, D, P, &s_fail); break;
+      }
+    }
     if (threadIdx.x == 0) info[idx] = f;
     if (f == 0 && do_solve) solve_one<T>(a, it.n, (T*)it.b);
     __syncthreads();
@@ -249,6 +269,7 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
     const int bucket = std::min(NBUCKETS - 1, items_in[j].n / 32);
     int blk = blk_table ? blk_table[bucket] : (sizeof(T) == 8 ? 32 : 64);
     blk = std::max(1, std::min(blk, sizeof(T) == 8 ? 32 : 64));
+    blk = blk <= 8 ? 8 : blk <= 16 ? 16 : blk <= 32 ? 32 : 64;  // the compiled widths
     items[i] = items_in[j];
     items[i].blk = blk;
     maxblk = std::max(maxblk, blk);
