@@ -43,6 +43,43 @@ __device__ __forceinline__ T tsqrt(T x) { return sqrt(x); }
 template <>
 __device__ __forceinline__ float tsqrt<float>(float x) { return sqrtf(x); }
 
+// Cholesky of the kb x kb (kb <= 32) block at rows/columns off.. of D (lower, column-major,
+// ld 65) in one warp: lane r holds row r in registers, and the current column is published
+// through the padding slots D[c * 65 + 64] (row 64 of D is never data), so the warp needs no
+// block-wide barrier.  A non-positive pivot is replaced by 1 so the steps stay finite;
+// returns the first one (kb if none), and writes the block back only if it factored.
+template <typename T>
+__device__ int chol32_warp(T* D, int off, int kb, int lane) {
+  T a[32];
+#pragma unroll
+  for (int c = 0; c < 32; c++)
+    a[c] = (lane < kb && c <= lane) ? D[(off + c) * 65 + off + lane] : ((c == lane) ? T(1) : T(0));
+  int bad = kb;
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    D[lane * 65 + 64] = a[j];  // column j as it stands
+    __syncwarp();
+    T d = D[j * 65 + 64];
+    if (!(d > T(0))) {
+      if (j < kb) bad = min(bad, j);
+      d = T(1);
+    }
+    const T sq = tsqrt(d), inv = T(1) / sq;
+    const T lj = (lane == j) ? sq : a[j] * inv;  // L(lane, j)
+    if (lane >= j) a[j] = lj;
+#pragma unroll
+    for (int c = j + 1; c < 32; c++)  // A(lane, c) -= L(lane, j) L(c, j)
+      if (lane >= c) a[c] -= lj * (D[c * 65 + 64] * inv);
+    __syncwarp();
+  }
+  if (bad == kb) {
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+      if (lane < kb && c <= lane) D[(off + c) * 65 + off + lane] = a[c];
+  }
+  return bad;
+}
+
 // Shared layout: D[64][65] (diagonal block), P[NMAX][blk+1] (panel copy).  BLK is the
 // panel width (a compile-time constant, so that the panel solve keeps its row in registers).
 template <typename T, int BLK>
@@ -59,23 +96,66 @@ __device__ int factor_one(T* __restrict__ A, int n, T* D, T* P, int* s_fail) {
     }
     if (t == 0) *s_fail = 0;
     __syncthreads();
-    for (int j = 0; j < kb; j++) {
-      if (t == 0) {
-        const T d = D[j * 65 + j];
-        if (!(d > T(0))) *s_fail = k + j + 1;
-        else D[j * 65 + j] = tsqrt(d);
+    if constexpr (sizeof(T) == 4) {
+      // FP32: in one warp for kb <= 32; a wider block as two 32-blocks: L11 (warp), L21 := A21 L11^-T
+      // (a thread per row), A22 -= L21 L21^T (all threads), L22 (warp)
+      if (t < 32) {
+        const int b = chol32_warp(D, 0, min(kb, 32), t);
+        if (t == 0 && b < min(kb, 32)) *s_fail = k + b + 1;
       }
       __syncthreads();
-      if (*s_fail) break;
-      const T inv = T(1) / D[j * 65 + j];
-      for (int r = j + 1 + t; r < kb; r += BT) D[j * 65 + r] *= inv;
-      __syncthreads();
-      const int w = kb - j - 1;
-      for (int idx = t; idx < w * w; idx += BT) {
-        const int c = j + 1 + idx / w, r = j + 1 + idx % w;
-        if (r >= c) D[c * 65 + r] -= D[j * 65 + r] * D[j * 65 + c];
+      if (kb > 32 && !*s_fail) {
+        if (t >= 32 && t < kb) {
+          T v[32];
+#pragma unroll
+          for (int c = 0; c < 32; c++) v[c] = D[c * 65 + t];
+#pragma unroll
+          for (int c = 0; c < 32; c++) {
+            T x = v[c];
+#pragma unroll
+            for (int q = 0; q < c; q++) x -= v[q] * D[q * 65 + c];
+            v[c] = x / D[c * 65 + c];
+          }
+#pragma unroll
+          for (int c = 0; c < 32; c++) D[c * 65 + t] = v[c];
+        }
+        __syncthreads();
+        const int w2 = kb - 32;
+        for (int idx = t; idx < w2 * w2; idx += BT) {
+          const int c = 32 + idx / w2, r = 32 + idx % w2;
+          if (r >= c) {
+            T acc = T(0);
+#pragma unroll 8
+            for (int q = 0; q < 32; q++) acc += D[q * 65 + r] * D[q * 65 + c];
+            D[c * 65 + r] -= acc;
+          }
+        }
+        __syncthreads();
+        if (t < 32) {
+          const int b = chol32_warp(D, 32, w2, t);
+          if (t == 0 && b < w2) *s_fail = k + 32 + b + 1;
+        }
+        __syncthreads();
       }
-      __syncthreads();
+    } else {  // FP64: column by column over the CTA (the warp form spills its doubles)
+      for (int j = 0; j < kb; j++) {
+        if (t == 0) {
+          const T d = D[j * 65 + j];
+          if (!(d > T(0))) *s_fail = k + j + 1;
+          else D[j * 65 + j] = tsqrt(d);
+        }
+        __syncthreads();
+        if (*s_fail) break;
+        const T inv = T(1) / D[j * 65 + j];
+        for (int r = j + 1 + t; r < kb; r += BT) D[j * 65 + r] *= inv;
+        __syncthreads();
+        const int w = kb - j - 1;
+        for (int idx = t; idx < w * w; idx += BT) {
+          const int c = j + 1 + idx / w, r = j + 1 + idx % w;
+          if (r >= c) D[c * 65 + r] -= D[j * 65 + r] * D[j * 65 + c];
+        }
+        __syncthreads();
+      }
     }
     for (int idx = t; idx < kb * kb; idx += BT) {
       const int c = idx / kb, r = idx % kb;
