@@ -2,10 +2,12 @@
 
     python -m oocdag_gb300.kernel_bench syrk  --m 8192 --k 512 --prec bf16x3 [--reps 3]
     python -m oocdag_gb300.kernel_bench mixed --n 16384 --nb 256 --prec bf16x3
+    python -m oocdag_gb300.kernel_bench batched --count 2000 --prec fp32 [--reps 2]
 
 ``syrk`` times one trailing-update launch C -= X X^T (lower, FP64 C) in the given
 precision and prints the useful FP64-equivalent rate and the C read+write bandwidth;
-``mixed`` times one mixed-precision factorization plus refinement of a seeded system.
+``mixed`` times one mixed-precision factorization plus refinement of a seeded system;
+``batched`` times the persistent batched factor + solve of `count` seeded small systems.
 These are the commands the profile summaries under profiles/ were captured with.
 """
 from __future__ import annotations
@@ -68,6 +70,29 @@ def mixed(args) -> None:
     h.close()
 
 
+def batched(args) -> None:
+    """`count` systems n ~ U{16..512} (numpy seed `seed`), A = M M^T / n + I, through the
+    persistent batched kernel `reps` times with the given panel-width table."""
+    import numpy as np
+
+    import oocdag_gb300 as ooc
+    from oocdag_gb300 import autotune
+
+    h = ooc.Handle(0)
+    rng = np.random.default_rng(args.seed)
+    ns = [int(x) for x in rng.integers(16, 513, size=args.count)]
+    A0, B0, a_off, b_off = autotune.make_batch(ns, 7, args.prec)
+    flops = sum(n ** 3 / 3 for n in ns)
+    for rep in range(args.reps):
+        A, B = A0.clone(), B0.clone()
+        info, sec = h.batched_posv(args.prec, ns, a_off, b_off, A, B, blk_table=args.table)
+        if any(info):
+            raise RuntimeError("a batched system failed")
+        print(json.dumps({"kind": "batched", "prec": args.prec, "count": args.count, "rep": rep, "seconds": sec,
+                          "tflops": flops / sec / 1e12}), flush=True)
+    h.close()
+
+
 def main() -> None:
     p = argparse.ArgumentParser()
     sub = p.add_subparsers(dest="cmd", required=True)
@@ -82,8 +107,15 @@ def main() -> None:
     b.add_argument("--delta", type=float, default=0.1)
     b.add_argument("--prec", nargs="+", default=["bf16x3"])
     b.add_argument("--reps", type=int, default=1)
+    c = sub.add_parser("batched")
+    c.add_argument("--count", type=int, default=2000)
+    c.add_argument("--prec", default="fp32", choices=["fp64", "fp32"])
+    c.add_argument("--seed", type=int, default=5)
+    c.add_argument("--reps", type=int, default=2)
+    c.add_argument("--table", type=int, nargs=16,
+                   default=[64, 32, 32, 32, 32, 32, 32, 32, 64, 64, 64, 64, 64, 64, 64, 64])
     args = p.parse_args()
-    {"syrk": syrk, "mixed": mixed}[args.cmd](args)
+    {"syrk": syrk, "mixed": mixed, "batched": batched}[args.cmd](args)
 
 
 if __name__ == "__main__":
