@@ -628,7 +628,8 @@ def run_mixed(args):
         upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk-update launch "
                                       "(kernel_bench mixed --n 16384), scaled to this workload's launches")
     chain_flops = sum(2 * LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in panels) * args.steps
-    fac_roof = {"kernel": "diagonal chain: k_diag_f32 (FP32 potrf + inverse of the 512x512 tile, one CTA) + "
+    fac_roof = {"kernel": "diagonal chain: k_diag_s256 / k_diag_f32 (FP32 potrf + inverse of the 256- / 512-wide "
+                          "diagonal tile, one CTA) + "
                           + ("k_trsm2_bf16x3 (split-BF16 tcgen05 column solve)" if args.prec == "bf16x3"
                              else "k_colsolve_f32 (FP32 column solve)"),
                 "bound": "latency (one CTA)",

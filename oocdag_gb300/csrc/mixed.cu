@@ -563,6 +563,266 @@ __global__ void __launch_bounds__(DG_THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------------
+// The same outputs for a diagonal tile of at most 256 columns, with the whole tile in
+// shared memory: its lower block triangle as 32 x 32 blocks (row-major, pitch 36), padded
+// to a multiple of 32 with the identity.  k_diag_f32 re-reads the finished columns from L2
+// in every step, and beside the trailing update (which loads L2 heavily) those round trips,
+// not its arithmetic, set its time; here no step waits on L2, and every block product runs
+// from registers (a 4 x 8 tile per lane, 16-byte shared loads).
+//   phase 1, block column K (right-looking): one warp factors L_KK in registers; one
+//            thread per row below solves its row against L_KK^T (the solved rows also
+//            go, transposed, into PT, and to D) while a warp forms X_KK = L_KK^{-1}; then
+//            each block (I, J), K < J <= I, takes -= L(I,K) L(J,K)^T, a warp a block.
+//   phase 2, X = L^{-1} in place (right-looking): block row K of X is X_KK times the
+//            finished block row; then each block (I, J), I > K, J <= K, takes
+//            -= L(I,K) X(K,J) (for J = K: := -L(I,K) X_KK).
+// Phase 2 runs one step behind phase 1, in the warps that the serial parts of phase 1
+// leave idle (its products of step K-1 beside the Cholesky of block K, while PT still holds
+// L(., K-1)), so the two phases share their barriers.
+// Dinv (= X^T), and X row-major as BF16 planes (or in FP32 into Xr when no planes are
+// asked for), at the end.  A non-positive pivot writes
+// info = col0 + j + 1 to the status word and stops, the columns left of the failed block
+// written, the others left as they were (as k_diag_f32).
+// ---------------------------------------------------------------------------------
+constexpr int DS_MAX = 256, DS_NBK = DS_MAX / DG_B, DS_P = 36, DS_BLK = DG_B * DS_P;
+constexpr int DS_NBLK = DS_NBK * (DS_NBK + 1) / 2;
+constexpr int DS_PTLD = DS_MAX - DG_B + 4;  // rows below a block column, 16-byte multiple
+constexpr size_t DS_SMEM =
+    (size_t)((DS_NBLK + DS_NBK) * DS_BLK + DG_B * DS_PTLD + 2 * DG_B) * sizeof(float);
+
+// block b of a lower block triangle stored row by row -> (I, J), J <= I
+__device__ __forceinline__ void ds_block_ij(int b, int& I, int& J) {
+  int i = (int)((sqrtf(8.f * (float)b + 1.f) - 1.f) * 0.5f);
+  if ((i + 1) * (i + 2) / 2 <= b) i++;
+  if (i * (i + 1) / 2 > b) i--;
+  I = i;
+  J = b - i * (i + 1) / 2;
+}
+
+// acc[i][j] += sum over k < 32 of A[k lda + r0 + i] B[k ldb + c0 + j]: lane's 4 x 8 tile of
+// a 32 x 32 block product (A and B k-major, rows 16-byte aligned)
+__device__ __forceinline__ void ds_mm32(float acc[4][8], const float* A, int lda, const float* B, int ldb, int r0,
+                                        int c0) {
+#pragma unroll 8
+  for (int k = 0; k < DG_B; k++) {
+    const float4 a = *reinterpret_cast<const float4*>(A + k * lda + r0);
+    const float4 b0 = *reinterpret_cast<const float4*>(B + k * ldb + c0);
+    const float4 b1 = *reinterpret_cast<const float4*>(B + k * ldb + c0 + 4);
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+  }
+}
+
+// the lane's tile of block C (pitch DS_P) := C - acc (mode 0), -acc (mode 1) or acc (mode 2)
+__device__ __forceinline__ void ds_put(float* C, const float acc[4][8], int r0, int c0, int mode) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    float4* p = reinterpret_cast<float4*>(C + (r0 + i) * DS_P + c0);
+    float v[8];
+    if (mode == 0) {
+      const float4 u = p[0], w = p[1];
+      const float cv[8] = {u.x, u.y, u.z, u.w, w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = cv[j] - acc[i][j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = (mode == 1) ? -acc[i][j] : acc[i][j];
+    }
+    p[0] = make_float4(v[0], v[1], v[2], v[3]);
+    p[1] = make_float4(v[4], v[5], v[6], v[7]);
+  }
+}
+
+// 32 x 32 Cholesky of a diagonal block (pitch DS_P) by one warp, in registers (lane r = row
+// r, as in k_diag_f32): the block's lower triangle := L (zeros above), dinv := 1 / diag(L).
+// Rows and columns from kb on are taken as the identity.  A non-positive pivot in the first
+// kb columns sets *fail and writes info = colg + j + 1 to the status word.
+__device__ __forceinline__ void ds_chol32(float* Tb, int kb, i64 colg, float* colb, float* dinv, int* fail,
+                                          int* status, int lane) {
+  float a[DG_B];
+#pragma unroll
+  for (int c = 0; c < DG_B; c++) a[c] = (lane < kb && c <= lane) ? Tb[lane * DS_P + c] : ((c == lane) ? 1.f : 0.f);
+  int first_bad = DG_B;
+#pragma unroll
+  for (int j = 0; j < DG_B; j++) {
+    colb[lane] = a[j];
+    __syncwarp();
+    float d = colb[j];
+    if (!(d > 0.f)) {
+      first_bad = min(first_bad, j);
+      d = 1.f;
+    }
+    const float inv = rsqrtf(d);
+    const float lj = (lane == j) ? d * inv : a[j] * inv;  // L(lane, j)
+    const float ljs = lj * inv;                             // L(lane, j) / sqrt(d)
+    if (lane == j) dinv[j] = inv;
+    a[j] = (lane >= j) ? lj : a[j];
+#pragma unroll
+    for (int c = j + 1; c < DG_B; c++)
+      if (lane >= c) a[c] = fmaf(-ljs, colb[c], a[c]);
+    __syncwarp();
+  }
+  if (first_bad < kb && lane == 0) {
+    *fail = 1;
+    atomicCAS(status, 0, (int)(colg + first_bad + 1));
+  }
+#pragma unroll
+  for (int c = 0; c < DG_B; c++) Tb[lane * DS_P + c] = (c <= lane) ? a[c] : 0.f;
+}
+
+__global__ void __launch_bounds__(DG_THREADS, 1)
+    k_diag_s256(float* D, i64 ldd, int LN, i64 col0, float* __restrict__ Dinv, i64 lde, float* __restrict__ Xr,
+                __nv_bfloat16* __restrict__ Xh, __nv_bfloat16* __restrict__ Xl, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(16) float dss[];
+  float* T = dss;                         // block (I, J) at (I (I + 1) / 2 + J) DS_BLK
+  float* XD = T + DS_NBLK * DS_BLK;       // X_KK transposed: XD[K DS_BLK + k DS_P + r] = X_KK(r, k)
+  float* PT = XD + DS_NBK * DS_BLK;       // block column K below its diagonal, transposed
+  float* dinv = PT + DG_B * DS_PTLD;      // 1 / L(k0 + c, k0 + c)
+  float* colb = dinv + DG_B;              // the warp Cholesky's column broadcast
+  __shared__ int s_fail;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int NBK = (LN + DG_B - 1) / DG_B;
+  const int r0 = (lane & 7) * 4, c0 = (lane >> 3) * 8;  // the lane's tile of a block product
+  auto blk = [&](int I, int J) -> float* { return T + (I * (I + 1) / 2 + J) * DS_BLK; };
+  if (t == 0) s_fail = 0;
+  {  // the lower block triangle, 24 loads in flight per thread (lanes down a column)
+    constexpr int U = 24;
+    const int total = NBK * (NBK + 1) / 2 * DG_B * DG_B;
+    for (int base = 0; base < total; base += U * DG_THREADS) {
+      float v[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int idx = base + u * DG_THREADS + t;
+        float x = 0.f;
+        if (idx < total) {
+          int I, J;
+          ds_block_ij(idx >> 10, I, J);
+          const int i = I * DG_B + (idx & 31), j = J * DG_B + ((idx >> 5) & 31);
+          if (i < LN && j < LN) {
+            if (i >= j) x = D[i + (i64)j * ldd];
+          } else if (i == j) {
+            x = 1.f;
+          }
+        }
+        v[u] = x;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int idx = base + u * DG_THREADS + t;
+        if (idx < total) T[(idx >> 10) * DS_BLK + (idx & 31) * DS_P + ((idx >> 5) & 31)] = v[u];
+      }
+    }
+  }
+  __syncthreads();
+  // ---- Phase 1 (L = chol(D)) step K and phase 2 (X = L^{-1}) step K-1 run together in
+  // iteration K: the phase-2 products of step K-1 beside the warp Cholesky of block K (PT
+  // still holds L(., K-1) transposed), and block row K of X beside the trailing update.
+  int K = 0;
+  for (; K < NBK; K++) {
+    const int k0 = K * DG_B, kb = min(DG_B, LN - k0), nI = NBK - 1 - K;
+    float* Tkk = blk(K, K);
+    if (warp == 0) {
+      ds_chol32(Tkk, kb, col0 + k0, colb, dinv, &s_fail, status, lane);
+    } else if (K > 0) {  // phase 2, step K-1: block (K+ii, J) -= L(K+ii, K-1) X(K-1, J), J < K-1;
+                         // block (K+ii, K-1) := -L(K+ii, K-1) X_{K-1}
+      for (int it = warp - 1; it < (NBK - K) * K; it += DG_WARPS - 1) {
+        const int ii = it / K, J = it - ii * K;
+        float acc[4][8] = {};
+        ds_mm32(acc, PT + ii * DG_B, DS_PTLD, blk(K - 1, J), DS_P, r0, c0);
+        ds_put(blk(K + ii, J), acc, r0, c0, J < K - 1 ? 0 : 1);
+      }
+    }
+    __syncthreads();
+    if (s_fail) return;  // D holds L left of block K (written below), the rest as it was
+    if (t < nI * DG_B) {  // row t below: B := B L_KK^{-T}, into the tile, PT and D
+      const int i = (K + 1) * DG_B + t;
+      float* Trow = blk(K + 1 + (t >> 5), K) + (t & 31) * DS_P;
+      float row[DG_B];
+#pragma unroll
+      for (int c4 = 0; c4 < DG_B / 4; c4++) {
+        const float4 q = reinterpret_cast<const float4*>(Trow)[c4];
+        row[4 * c4 + 0] = q.x;
+        row[4 * c4 + 1] = q.y;
+        row[4 * c4 + 2] = q.z;
+        row[4 * c4 + 3] = q.w;
+      }
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) {
+        float v = row[c];
+#pragma unroll
+        for (int q = 0; q < c; q++) v = fmaf(-row[q], Tkk[c * DS_P + q], v);
+        row[c] = v * dinv[c];
+      }
+#pragma unroll
+      for (int c4 = 0; c4 < DG_B / 4; c4++)
+        reinterpret_cast<float4*>(Trow)[c4] =
+            make_float4(row[4 * c4 + 0], row[4 * c4 + 1], row[4 * c4 + 2], row[4 * c4 + 3]);
+#pragma unroll
+      for (int c = 0; c < DG_B; c++) PT[c * DS_PTLD + t] = row[c];
+      if (i < LN) {  // a block column with rows below is full width
+#pragma unroll
+        for (int c = 0; c < DG_B; c++) D[i + (i64)(k0 + c) * ldd] = row[c];
+      }
+    } else if (warp == DG_WARPS - 1) {  // X_KK by columns: lane c solves L_KK x = e_c
+      float x[DG_B];
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) {
+        float v = (r == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int q = 0; q < r; q++) v = fmaf(-Tkk[r * DS_P + q], x[q], v);
+        x[r] = v * dinv[r];
+      }
+      float* Xk = XD + K * DS_BLK;
+#pragma unroll
+      for (int r = 0; r < DG_B; r++) Xk[lane * DS_P + r] = x[r];
+    } else if (warp == DG_WARPS - 2) {  // L_KK into D, lanes down the rows
+      for (int c = 0; c < kb; c++)
+        if (lane >= c && lane < kb) D[(k0 + lane) + (i64)(k0 + c) * ldd] = Tkk[lane * DS_P + c];
+    }
+    __syncthreads();
+    // trailing lower block triangle: block (K+1+ii, K+1+jj) -= L(., K) L(., K)^T; then phase
+    // 2, step K: X(K, J) = X_KK B(K, J) for J < K (B(K, J) is final), and X(K, K) = X_KK
+    const int ntr = nI * (nI + 1) / 2;
+    for (int it = warp; it <= ntr + K; it += DG_WARPS) {
+      if (it < ntr) {
+        int ii, jj;
+        ds_block_ij(it, ii, jj);
+        float acc[4][8] = {};
+        ds_mm32(acc, PT + ii * DG_B, DS_PTLD, PT + jj * DG_B, DS_PTLD, r0, c0);
+        ds_put(blk(K + 1 + ii, K + 1 + jj), acc, r0, c0, 0);
+      } else {
+        const float* Xk = XD + K * DS_BLK;
+        const int J = it - ntr;
+        if (J < K) {
+          float* Bkj = blk(K, J);
+          float acc[4][8] = {};
+          ds_mm32(acc, Xk, DS_P, Bkj, DS_P, r0, c0);
+          __syncwarp();
+          ds_put(Bkj, acc, r0, c0, 2);
+        } else {
+#pragma unroll 4
+          for (int c = 0; c < DG_B; c++) Tkk[lane * DS_P + c] = (c <= lane) ? Xk[c * DS_P + lane] : 0.f;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // Dinv = X^T (zeros below its diagonal), X row-major as BF16 planes or in FP32
+  for (int i = warp; i < LN; i += DG_WARPS)
+    for (int j = lane; j < LN; j += 32) {
+      const float x = (j <= i) ? blk(i >> 5, j >> 5)[(i & 31) * DS_P + (j & 31)] : 0.f;
+      Dinv[j + (i64)i * lde] = x;
+      if (Xh) dg_split_store(Xh, Xl, (i64)i * LN + j, x);
+      else Xr[(i64)i * LN + j] = x;
+    }
+}
+
 // FP32 column panel (m x K, ld ldx) -> copy with ld ldy.
 __global__ void k_copy_f32(const float* __restrict__ X, i64 ldx, float* __restrict__ Y, i64 ldy, int m, int K) {
   const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1595,6 +1855,7 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     if ((rc = F->work.ensure(pb)) || (rc = F->work2.ensure(pb))) return rc;
   }
   OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_s256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DS_SMEM));
   cudaEvent_t evA, evP;  // A: next panel's columns updated (s0 -> s1); P: diagonal tile done (s1 -> s0)
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evA, cudaEventDisableTiming));
   OOC_CUDA_TRY(cudaEventCreateWithFlags(&evP, cudaEventDisableTiming));
@@ -1624,7 +1885,10 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
     float* Djj = A + J0 + J0 * lda;
     OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
     if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
-    k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
+    if (LN <= DS_MAX)  // the tile fits in shared memory
+      k_diag_s256<<<1, DG_THREADS, DS_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
+    else
+      k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
     OOC_CUDA_TRY(cudaGetLastError());
     if (prof->on) prof->mark(s1);
     OOC_CUDA_TRY(cudaEventRecord(evP, s1));
