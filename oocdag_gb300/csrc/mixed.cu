@@ -975,7 +975,16 @@ __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A,
     }                                                                         // consecutive kk
     __syncthreads();
     if (row < m) {
-      int kk = lane;
+      int kk = lane;  // eight loads in flight, then four, then one (k ascending either way)
+      for (; kk + 224 < kn; kk += 256) {
+        TC a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] = (TC)Acol[kc + kk + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+          for (int q = 0; q < R; q++) acc[q] = fma(a[u], Bs[q * NN_KCHUNK + kk + 32 * u], acc[q]);
+      }
       for (; kk + 96 < kn; kk += 128) {
         TC a[4];
 #pragma unroll
@@ -1004,6 +1013,72 @@ __global__ void __launch_bounds__(256) k_gemm_tn_small(const TA* __restrict__ A,
     if (q >= r) break;
     TC* c = C + row + (i64)q * ldc;
     *c = (beta != TC(0)) ? fma(alpha, acc[q], *c) : alpha * acc[q];
+  }
+}
+
+// One right-hand side through a diagonal block's inverse: x = U^T b (TRANS) or x = U b,
+// U = Dinv_J = L_JJ^{-T} (LN x LN, ld ldu, upper triangular), so output i takes only
+// k <= i (TRANS) or k >= i.  CTA = 32 outputs x 16 warps, warp w takes k in [32w, 32w+32):
+// all of a thread's loads are issued before its first FMA (one round trip instead of a
+// walk), the 16 warp sums added in warp order.  TRANS: lane = k, 32 outputs per lane, then
+// a transposing butterfly leaves lane l with its warp's sum for output l; otherwise lane =
+// output row, b(k) passed along the warp by shuffles.  LN <= 512.
+constexpr int DMV_WARPS = 16;
+// a[0..S) := the lane's kept half plus the partner's passed half (partner = lane ^ S)
+template <typename T, int S>
+__device__ __forceinline__ void dmv_fold(T (&a)[32], int lane) {
+  const bool hi = (lane & S) != 0;
+#pragma unroll
+  for (int j = 0; j < S; j++) {
+    const T send = hi ? a[j] : a[j + S];
+    const T keep = hi ? a[j + S] : a[j];
+    a[j] = keep + __shfl_xor_sync(0xffffffffu, send, S);
+  }
+}
+
+template <typename T, bool TRANS>
+__global__ void __launch_bounds__(DMV_WARPS * 32) k_dinv_mv(const T* __restrict__ U, i64 ldu, int LN,
+                                                           const T* __restrict__ b, T* __restrict__ x) {
+  __shared__ T part[DMV_WARPS][33];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = blockIdx.x * 32, k0 = warp * 32;
+  const int kl = k0 + lane;
+  const T bk = (kl < LN) ? b[kl] : T(0);
+  T acc;
+  if (TRANS) {
+    T a[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      const int i = i0 + j;
+      a[j] = (kl < LN && i < LN && kl <= i) ? U[kl + (i64)i * ldu] : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < 32; j++) a[j] *= bk;
+    dmv_fold<T, 16>(a, lane);  // keep half, pass half: lane l ends with index l
+    dmv_fold<T, 8>(a, lane);
+    dmv_fold<T, 4>(a, lane);
+    dmv_fold<T, 2>(a, lane);
+    dmv_fold<T, 1>(a, lane);
+    acc = a[0];
+  } else {
+    const int i = i0 + lane;
+    T v[32];
+#pragma unroll
+    for (int u = 0; u < 32; u++) {
+      const int k = k0 + u;
+      v[u] = (i < LN && k < LN && k >= i) ? U[i + (i64)k * ldu] : T(0);
+    }
+    acc = T(0);
+#pragma unroll
+    for (int u = 0; u < 32; u++) acc = fma(v[u], __shfl_sync(0xffffffffu, bk, u), acc);
+  }
+  part[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && i0 + lane < LN) {
+    T sum = part[0][lane];
+#pragma unroll
+    for (int w = 1; w < DMV_WARPS; w++) sum += part[w][lane];
+    x[i0 + lane] = sum;
   }
 }
 
@@ -1600,8 +1675,13 @@ int solve_with(const T* L, i64 ldl, const T* Dinv, const Panels& P, T* B, i64 ld
     i64 J0, off;
     int LN, ld;
     P.get(J, &J0, &LN, &off, &ld);
-    rc = gemm_tn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s);  // Dinv_J^T b_J
-    if (rc) return rc;
+    if (r == 1 && LN <= DMV_WARPS * 32) {  // Dinv_J^T b_J
+      k_dinv_mv<T, true><<<(LN + 31) / 32, DMV_WARPS * 32, 0, s>>>(Dinv + off, ld, LN, B + J0, tmp);
+      OOC_CUDA_TRY(cudaGetLastError());
+    } else {
+      rc = gemm_tn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s);
+      if (rc) return rc;
+    }
     const i64 rows = n - J0 - LN;
     if (rows > 0) {
       rc = gemm_nn_small<T, T>(L + (J0 + LN) + J0 * ldl, ldl, tmp, nt, B + J0 + LN, ldb, (int)rows, LN, r, T(-1),
@@ -1617,8 +1697,13 @@ int solve_with(const T* L, i64 ldl, const T* Dinv, const Panels& P, T* B, i64 ld
     i64 J0, off;
     int LN, ld;
     P.get(J, &J0, &LN, &off, &ld);
-    rc = gemm_nn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s, nullptr);
-    if (rc) return rc;
+    if (r == 1 && LN <= DMV_WARPS * 32) {  // Dinv_J y_J
+      k_dinv_mv<T, false><<<(LN + 31) / 32, DMV_WARPS * 32, 0, s>>>(Dinv + off, ld, LN, B + J0, tmp);
+      OOC_CUDA_TRY(cudaGetLastError());
+    } else {
+      rc = gemm_nn_small<T, T>(Dinv + off, ld, B + J0, ldb, tmp, nt, LN, LN, r, T(1), T(0), s, nullptr);
+      if (rc) return rc;
+    }
     if (J0 > 0) {  // y_{<J} -= L_{J,<J}^T x_J
       rc = gemm_tn_small<T, T>(L + J0, ldl, tmp, nt, B, ldb, (int)J0, LN, r, T(-1), T(1), s,
                                CopyOut<T>{tmp, nt, B + J0, ldb, LN});
