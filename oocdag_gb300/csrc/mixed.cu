@@ -1116,13 +1116,24 @@ __global__ void k_lower_conv(const TS* __restrict__ S, i64 lds, TD* __restrict__
                              int zero_upper) {
   const i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  for (int cc = blockIdx.y; cc < w; cc += gridDim.y) {
-    const i64 c = c0 + cc;
-    if (r >= c) {
-      if constexpr (sizeof(TD) == 4) D[r + cc * ldd] = to_f32(S[r + cc * lds]);
-      else D[r + cc * ldd] = to_f64(S[r + cc * lds]);
-    } else if (zero_upper) {
-      D[r + cc * ldd] = TD(0);
+  constexpr int U = 4;  // columns per pass, their loads issued before the first store
+  for (int cb = blockIdx.y; cb < w; cb += U * gridDim.y) {
+    TS v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int cc = cb + u * gridDim.y;
+      v[u] = (cc < w && r >= c0 + cc) ? S[r + (i64)cc * lds] : TS(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int cc = cb + u * gridDim.y;
+      if (cc >= w) break;
+      if (r >= c0 + cc) {
+        if constexpr (sizeof(TD) == 4) D[r + (i64)cc * ldd] = to_f32(v[u]);
+        else D[r + (i64)cc * ldd] = to_f64(v[u]);
+      } else if (zero_upper) {
+        D[r + (i64)cc * ldd] = TD(0);
+      }
     }
   }
 }
