@@ -2,16 +2,17 @@
 
 One JSON line on rank 0.  Two forms (``--form``):
 
-* ``mixed`` (default; BASELINE configs[2]: n=65536, nb=512, A = (R+R^T)/2 + alpha I with
-  alpha = 0.5774 sqrt(n) (1+delta), delta = 0.1, one N(0,1) right-hand side).  A step is
-  one factorization with split-BF16 tensor-core trailing updates (FP64 diagonal potrf and
-  column solve) followed by FP64 iterative refinement to a normwise backward error
-  <= 1e-14.  ``value`` = n^3/3 / step time with A resident in HBM; ``fp64`` = the same
-  solve done by the plain FP64 path, measured once; the forward and backward errors of
-  every solve are reported per delta.  configs[1] (n=163840, 214.7 GB pinned host matrix)
-  does not fit this machine's host RAM (209 GB in total) and is not run.
-* ``fp64-ooc``: the plain FP64 out-of-core factorization (C1 geometry at n=24576,
-  nb=1024, 1 GiB device budget for the host leg).
+* ``mixed`` (default: n=65536, nb=512, A = (R+R^T)/2 + alpha I with alpha = 0.5774
+  sqrt(n) (1+delta), delta = 0.1, one N(0,1) right-hand side).  A step is one
+  factorization in an FP32 working matrix (FP32 diagonal tiles, split-BF16 tensor-core
+  column solves and trailing updates) followed by FP64 iterative refinement to a normwise
+  backward error <= 1e-14.  ``value`` = n^3/3 / step time with A resident in HBM;
+  ``fp64`` = the same solve done by the plain FP64 path, measured once; the forward and
+  backward errors of every solve are reported per delta.  The plain FP64 out-of-core case at n=163840
+  (214.7 GB pinned host matrix) does not fit the host RAM of these boxes (209 GB in
+  total) and is not run.
+* ``fp64-ooc``: the plain FP64 out-of-core factorization at n=24576 with the 1024-wide
+  tiles of the n=163840 case and a 1 GiB device budget for the host leg.
 
 Common keys: ``e2e`` is the same metric through the C-ABI with host buffers (page-locked),
 host<->device copies inside the timed region; ``roofline`` reports the dominant kernel
@@ -42,8 +43,8 @@ METRIC = "Cholesky TFLOP/s (n^3/3 flops), mixed vs FP64 at backward err<=1e-14; 
 
 # DRAM bytes per algorithmic flop of k_panel_update, from one ncu capture of two launches
 # at n=8192, nb=1024 (dram__bytes_read.sum + dram__bytes_write.sum = 348.1 MB for
-# 44.02 GFLOP; profiles/k_panel_update_fp64_n8192.md).  The kernel's traffic is the
-# operand and C tiles, which scale with the flops of a launch at fixed nb.
+# 44.02 GFLOP).  The kernel's traffic is the operand and C tiles, which scale with the
+# flops of a launch at fixed nb.
 UPDATE_DRAM_BYTES_PER_FLOP = 348.1e6 / 44.02e9
 UPDATE_TRAFFIC_RATIO = 967.5 / 976.3  # k_syrk2_bf16x3 bulk launch, n=16384: ncu DRAM bytes / algorithmic bytes
 
@@ -66,7 +67,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-ref", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
-    p.add_argument("--no-extra", action="store_true", help="skip the configs[3] batched and configs[4] serving runs")
+    p.add_argument("--no-extra", action="store_true", help="skip the batched small-system and served request-stream runs")
     a = p.parse_args()
     if a.n is None:
         a.n = 65536 if a.form == "mixed" else 24576
@@ -245,10 +246,10 @@ def run_reference(args):
 
 def _workload_name(args) -> str:
     if args.form == "mixed":
-        return (f"configs[2]: mixed-precision ({args.prec} trailing updates, FP64 potrf/trsm) factor + FP64 "
+        return (f"mixed-precision factor (FP32 diagonal tiles, {args.prec} column solves and trailing updates) + FP64 "
                 f"iterative-refinement solve to backward error <= 1e-14, n={args.n}, nb={args.nb}, "
                 f"delta={args.delta}, nrhs={args.nrhs}")
-    return (f"plain FP64 out-of-core lower Cholesky n={args.n} nb={args.nb} (C1 tile size; e2e: host A, device "
+    return (f"plain FP64 out-of-core lower Cholesky n={args.n} nb={args.nb} (1024-wide tiles; e2e: host A, device "
             f"budget {args.budget_mb} MiB)")
 
 
@@ -428,7 +429,7 @@ def _measured_peaks() -> dict:
 
 
 def run_mixed(args):
-    """configs[2]: mixed factor + FP64 refinement, with the plain FP64 solve beside it."""
+    """Mixed factor + FP64 refinement, with the plain FP64 solve beside it."""
     rank, world, local = _init_dist()
     import numpy as np
     import torch
@@ -659,8 +660,8 @@ def run_mixed(args):
 
     extra = {}
     if rank == 0 and world == 1 and not args.no_extra:
-        for name, fn in (("batched_configs3", lambda: bench_batched(h, args)),
-                         ("serving_configs4", lambda: bench_serving(args))):
+        for name, fn in (("batched", lambda: bench_batched(h, args)),
+                         ("serving", lambda: bench_serving(args))):
             try:
                 extra[name] = fn()
             except Exception as e:  # report, do not lose the headline
@@ -693,7 +694,7 @@ def run_mixed(args):
 
 
 # ----------------------------------------------------------------------------------
-# configs[3]: batched small systems in one persistent launch
+# batched small systems (20,000, n in [16, 512]) in one persistent launch
 # ----------------------------------------------------------------------------------
 def panel_schedule(n, nb, prec, tail_order):
     """(J0, width) of the factor's panels, as the library schedules them: nb wide, and for
@@ -819,7 +820,7 @@ def bench_batched(h, args, count=20000, reps=3):
 
 
 # ----------------------------------------------------------------------------------
-# configs[4]: the served request stream
+# the served request stream
 # ----------------------------------------------------------------------------------
 def make_trace(rate, seconds, seed, big_frac=0.01, repeat_frac=0.3, nmin=64, nmax=32768, nbig=131072):
     import numpy as np
@@ -882,7 +883,7 @@ def run_trace(trace, prec, drain_s, workers=4, nb=512):
 
 
 def bench_serving(args, seconds=10.0, drain_s=20.0):
-    """configs[4]: Poisson 200 req/s, n log-uniform [64, 32768] + 1% n=131072, 30% repeats;
+    """Poisson 200 req/s, n log-uniform [64, 32768] + 1% n=131072, 30% repeats;
     mixed form beside the plain FP64 form; plus a sustainable-rate run of the same mix
     without the n=131072 requests, where the latency percentiles are meaningful."""
     out = {"rate_req_s": 200, "seconds_of_arrivals": seconds, "drain_s": drain_s}

@@ -1,4 +1,4 @@
-"""GPU tests of the batched persistent factor + solve (C3-style inputs, small batches).
+"""GPU tests of the batched persistent factor + solve (A = M M^T/n + I, n in [16, 512], small batches).
 
 Each matrix is compared with the per-matrix FP64 path (LAPACK via numpy on the same
 matrix): factor entries to FACT_TOL relative, solution to SOL_TOL relative; FP32 to the

@@ -2,8 +2,9 @@
 
 Bars: the plain-precision factor object reproduces the plain path bit for bit; solves
 agree with the oracle's FP64 solve (LAPACK dpotrs on the oracle factor) to a forward
-error of FWD_TOL; refinement reaches the normwise backward error BERR_TOL (1e-14, the
-spec bar) for every precision and every conditioning of the C2 generator.
+error of FWD_TOL; refinement reaches the normwise backward error BERR_TOL (1e-14) for
+every precision and every conditioning of the generator A = (R+R^T)/2 + alpha I,
+alpha = 0.5774 sqrt(n) (1+delta).
 """
 import math
 

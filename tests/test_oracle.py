@@ -31,7 +31,7 @@ def test_panel_plans_match_literal_find_yn(oracle_mod):
     for label, v in plans.items():
         got = oracle_mod.panel_plan(v["N"], v["NB"], v["memBlock"])
         assert got == [tuple(p) for p in v["panels"]], label
-    # The survey's C1 geometry: five panels starting (0,160,17),(17,143,20),(37,123,24).
+    # n=163840, nb=1024, 24e9-byte budget: five panels starting (0,160,17),(17,143,20),(37,123,24).
     c1 = plans["c1_n163840_nb1024_24e9B"]["panels"]
     assert len(c1) == 5 and [tuple(p) for p in c1[:3]] == [(0, 160, 17), (17, 143, 20), (37, 123, 24)]
     assert tuple(c1[-1]) == (94, 66, 66)
