@@ -590,6 +590,8 @@ constexpr int DS_NBLK = DS_NBK * (DS_NBK + 1) / 2;
 constexpr int DS_PTLD = DS_MAX - DG_B + 4;  // rows below a block column, 16-byte multiple
 constexpr size_t DS_SMEM =
     (size_t)((DS_NBLK + DS_NBK) * DS_BLK + DG_B * DS_PTLD + 2 * DG_B) * sizeof(float);
+static_assert(DS_SMEM + 64 <= 227 * 1024 && DG_SMEM + 64 <= 227 * 1024,
+              "a diagonal kernel's shared memory exceeds the 227 KB a CTA may opt in to");
 
 // block b of a lower block triangle stored row by row -> (I, J), J <= I
 __device__ __forceinline__ void ds_block_ij(int b, int& I, int& J) {
