@@ -348,7 +348,12 @@ extern "C" int ooc_fp64_peak_probe(ooc_handle* h, double ms, double* tflops) {
     k_dmma_probe<<<blocks, threads, 0, s>>>(out, iters);
     cudaEventRecord(e1, s);
     int rc = ooc_wait_stream(h, s);
-    if (rc) { cudaFree(out); return rc; }
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaFree(out);
+      return rc;
+    }
     cudaEventElapsedTime(&el, e0, e1);
     double flops = 2.0 * 8 * 8 * 4 * 8.0 * iters * (double)blocks * (threads / 32);
     rate = flops / (el * 1e-3) / 1e12;

@@ -2451,10 +2451,15 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, Rf, n, (int)n, r);
     rc = solve32();
     if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>(Rf, n, X, ldx, (int)n, r);
-  } else if (!rc) {
-    OOC_CUDA_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
-                                   cudaMemcpyDeviceToDevice, s));
-    rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), X, ldx, r, F->tmp, s, &F->part);
+  } else if (!rc) {  // (no early return: the buffers above are freed at the end)
+    const cudaError_t e = cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), r,
+                                            cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) {
+      ooc_set_last_error(e, "cudaMemcpy2DAsync (X := B)", __FILE__, __LINE__);
+      rc = OOC_ERR_CUDA;
+    } else {
+      rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), X, ldx, r, F->tmp, s, &F->part);
+    }
   }
   if (!rc) rc = ooc_wait_stream(h, s2);
   if (!rc) {

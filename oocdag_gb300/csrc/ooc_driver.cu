@@ -632,9 +632,15 @@ extern "C" int ooc_dpotrf_L(ooc_handle* h, double* A, int64_t n, int64_t lda, in
   h->ev_next = 0;
   h->prof_next = 0;
   int rc = OOC_OK;
-  OOC_CUDA_TRY(cudaMemsetAsync(h->d_status, 0, sizeof(int), h->s_comp));
+  {  // (no early return: a host matrix registered above is unregistered below)
+    const cudaError_t e = cudaMemsetAsync(h->d_status, 0, sizeof(int), h->s_comp);
+    if (e != cudaSuccess) {
+      ooc_set_last_error(e, "cudaMemsetAsync (status word)", __FILE__, __LINE__);
+      rc = OOC_ERR_CUDA;
+    }
+  }
   *h->h_status = 0;
-  rc = ooc_wait_stream(h, h->s_comp);
+  if (!rc) rc = ooc_wait_stream(h, h->s_comp);
   auto t0 = std::chrono::steady_clock::now();
   if (!rc) rc = on_device ? dpotrf_device(R, A, n, lda, nb) : dpotrf_host(R, A, n, lda, nb, dev_budget);
   int rc2 = sync_all(h);
