@@ -72,3 +72,62 @@ def test_entry_point_argument_checks_need_no_gpu(ooc):
     # NULL handle -> argument 1 invalid; never a crash
     assert L.ooc_dpotrf_L(None, None, 10, 10, 4, 0, ctypes.byref(info), None) == -1
     assert L.ooc_set_option(None, 1, 2) == -1
+
+
+def test_every_entry_point_checks_its_handle_first(ooc):
+    """A NULL handle (or factor, or server) is argument 1 invalid (-1) at every entry point,
+    and the destroy calls accept NULL; none of this touches a device."""
+    from oocdag_gb300 import server
+
+    L = ooc.load()
+    b = ctypes.byref
+    info, it = ctypes.c_int(0), ctypes.c_int(0)
+    F = ctypes.c_void_p()
+    d = ctypes.c_double(0)
+    v = ctypes.c_int64(0)
+    buf = (ctypes.c_double * 16)()
+    ns = (ctypes.c_int * 1)(4)
+    off = (ctypes.c_int64 * 1)(0)
+    assert L.ooc_spotrf_L(None, None, 10, 10, 4, 0, b(info), None) == -1
+    assert L.ooc_factor_create(None, buf, 4, 4, 4, ooc.PREC_BF16X3, b(F), b(info), None) == -1
+    assert L.ooc_factor_create_gen(None, 4, 1, 1.0, 4, ooc.PREC_FP64, b(F), b(info), None) == -1
+    assert L.ooc_solve_refine(None, None, buf, 4, buf, 4, buf, 4, 1, 1e-14, 5, b(it), b(d)) == -1
+    assert L.ooc_solve_refine_gen(None, None, 1, 1.0, buf, 4, buf, 4, 1, 1e-14, 5, b(it), b(d)) == -1
+    assert L.ooc_factor_solve(None, None, buf, 4, 1) == -1
+    assert L.ooc_factor_copy_L(None, buf, 4) == -1
+    assert L.ooc_factor_destroy(None) == ooc.OOC_OK
+    assert L.ooc_dsyrk_ln(None, ooc.PREC_FP64, 4, 4, buf, 4, buf, 4) == -1
+    assert L.ooc_gen_normal(None, buf, 4, 4, 1, 1) == -1
+    assert L.ooc_dmatgen_pdmatgen(None, buf, 4, 4, 2) == -1
+    assert L.ooc_dmatgen_uniform(None, buf, 4, 4, 1, 1.0) == -1
+    assert L.ooc_dresidual(None, buf, 4, 4, 2, 1, 1.0, b(d)) == -1
+    assert L.ooc_fp64_peak_probe(None, 1.0, b(d)) == -1
+    assert L.ooc_batched_dposv(None, 1, ns, off, off, buf, buf, b(info), None, 0, b(d)) == -1
+    assert L.ooc_batched_sposv(None, 1, ns, off, off, buf, buf, b(info), None, 0, b(d)) == -1
+    assert L.ooc_get_option(None, ooc.OPT_TAIL_ORDER, b(v)) == -1
+    assert L.ooc_last_info(None) == 0
+    assert L.ooc_destroy(None) == ooc.OOC_OK
+    assert L.ooc_dpotrf_L_static(None, 10, 10, 4, None, b(info)) == -1  # NULL matrix, n > 0
+    S = server._lib()
+    cnt, p64 = ctypes.c_int(0), ctypes.c_int64(0)
+    assert S.ooc_server_create(None, b(ctypes.c_void_p())) == -1
+    assert S.ooc_server_submit(None, b(server.Request(0, 64, 1, 2, 1, 0)), b(p64)) == -1
+    assert S.ooc_server_poll(None, None, 0, b(cnt), 0) == -1
+    assert S.ooc_server_solution(None, 1, buf, 4) == -1
+    assert S.ooc_server_status(None, b(p64), b(p64), b(p64), b(p64)) == -1
+    assert S.ooc_server_now(None) == 0.0
+    assert S.ooc_server_destroy(None) == ooc.OOC_OK
+
+
+def test_factor_bytes_accounting(ooc):
+    """The device bytes a factor object needs (host arithmetic): 4 n^2 + O(n nb) for the
+    reduced precisions (FP32 working matrix), more for FP64 (n^2 doubles plus the inverses)."""
+    L = ooc.load()
+    for n, nb in [(65536, 512), (4096, 256), (1001, 128)]:
+        b16 = L.ooc_factor_bytes(n, nb, ooc.PREC_BF16X3)
+        b32 = L.ooc_factor_bytes(n, nb, ooc.PREC_FP32)
+        b64 = L.ooc_factor_bytes(n, nb, ooc.PREC_FP64)
+        assert 4 * n * n <= b32 <= b16 < 4 * n * n + 64 * n * nb + (64 << 20)
+        assert b64 >= 8 * n * n
+    assert L.ooc_factor_bytes(65536, 512, ooc.PREC_BF16X3) < 18 * 10 ** 9  # fits beside A in 280 GB
+    assert L.ooc_factor_bytes(0, 512, ooc.PREC_FP64) == 0 and L.ooc_factor_bytes(16, 0, ooc.PREC_FP64) == 0
