@@ -466,6 +466,7 @@ def run_mixed(args):
 
     for _ in range(args.warmup):
         solve(args.prec)
+    npanels = len(panel_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER)))
     h.set_option(ooc.OPT_PROFILE, 1)
     clocks = ClockSampler(local)
     clocks.start()
@@ -486,7 +487,7 @@ def run_mixed(args):
         upd_launch += st["update_launches"]
         fac_ms += st["factor_ms"]
         fac_s += st["seconds"]
-        launches += st["kernel_launches"]
+        launches += st["kernel_launches"] + 1 + refine_launches(it, npanels)  # + the FP64->FP32 conversion
     e1.record(comp)
     torch.cuda.synchronize()
     barrier(world)
@@ -696,6 +697,18 @@ def run_mixed(args):
 # ----------------------------------------------------------------------------------
 # batched small systems (20,000, n in [16, 512]) in one persistent launch
 # ----------------------------------------------------------------------------------
+def refine_launches(iters, npanels):
+    """Kernels one ooc_solve_refine call launches on an FP32 or split-BF16 factor (device
+    A, up to 16 right-hand sides), from its structure: the norm of A (three residual-pass
+    kernels and a column maximum), the maximum of B, X0 (two conversions and a triangular
+    solve), per residual evaluation (iters + 1 of them) an initialisation, three pass
+    kernels and two column maxima, and per correction two conversions and a solve.  A
+    solve is two kernels per panel and sweep, less the one copy per sweep that replaces
+    the last panel's product."""
+    solve = 4 * npanels - 2
+    return 4 + 1 + (2 + solve) + 6 * (iters + 1) + iters * (2 + solve)
+
+
 def panel_schedule(n, nb, prec, tail_order):
     """(J0, width) of the factor's panels, as the library schedules them: nb wide, and for
     split-BF16 factors with nb a multiple of 256 nb/2 wide from the first multiple of nb at
