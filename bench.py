@@ -624,11 +624,11 @@ def run_mixed(args):
         upd_roof["frac"] = upd_roof["achieved"] / upd_roof["peak"]
     if args.prec == "bf16x3" and upd_launch:
         # DRAM bytes per launch: the algorithmic kernel bytes scaled by the measured/algorithmic
-        # ratio of one ncu capture (bulk update at n=16384, m=15872, block columns 4..:
+        # ratio of one ncu capture (bulk update at n=16384 with 512-wide panels, m=15872, block columns 4..:
         # 967.5 MB measured, 976.3 MB algorithmic)
         upd_roof["traffic"] = UPDATE_TRAFFIC_RATIO * kern_bytes / upd_launch
         upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk-update launch "
-                                      "(kernel_bench mixed --n 16384), scaled to this workload's launches")
+                                      "(kernel_bench mixed --n 16384 --nb 512 --tail-order 0), scaled to this workload's launches")
     chain_flops = sum(2 * LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in panels) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_s256 / k_diag_f32 (FP32 potrf + inverse of the 256- / 512-wide "
                           "diagonal tile, one CTA) + "

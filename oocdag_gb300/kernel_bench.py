@@ -54,6 +54,8 @@ def mixed(args) -> None:
     import oocdag_gb300 as ooc
 
     h = ooc.Handle(0)
+    if args.tail_order is not None:  # orders factored with nb/2-wide panels (0: uniform nb)
+        h.set_option(ooc.OPT_TAIL_ORDER, args.tail_order)
     n, nb = args.n, args.nb
     alpha = 0.5774 * math.sqrt(n) * (1 + args.delta)
     B = torch.empty((1, n), dtype=torch.float64, device="cuda")
@@ -107,6 +109,8 @@ def main() -> None:
     b.add_argument("--delta", type=float, default=0.1)
     b.add_argument("--prec", nargs="+", default=["bf16x3"])
     b.add_argument("--reps", type=int, default=1)
+    b.add_argument("--tail-order", type=int, default=None,
+                   help="OOC_OPT_TAIL_ORDER for the factor (default: the library's; 0: uniform nb-wide panels)")
     c = sub.add_parser("batched")
     c.add_argument("--count", type=int, default=2000)
     c.add_argument("--prec", default="fp32", choices=["fp64", "fp32"])
