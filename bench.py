@@ -895,6 +895,30 @@ def run_trace(trace, prec, drain_s, workers=4, nb=512):
     return res
 
 
+def cpu_request_times(sizes=(64, 256, 1024, 4096, 16384), seed=11, threads=None):
+    """The CPU path's time for one request of the served mix, per order: the oracle's
+    factorization (the reference's task graph on host BLAS, all host threads) and dpotrs
+    of A = (R+R^T)/2 + n I with one right-hand side.  The served stream has no CPU
+    counterpart; these single-request times stand beside its latencies."""
+    import numpy as np
+
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    oracle.set_blas_threads(1)
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in sizes:
+        nb = min(n, 256 if n <= 4096 else 512)
+        A = oracle.gen_uniform(n, seed, float(n))
+        b = rng.standard_normal((n, 1))
+        t0 = time.perf_counter()
+        _, info, _ = oracle.cholesky(A, nb, 1 << 40, threads, 2)
+        oracle.potrs(A, b)
+        out.append({"n": n, "nb": nb, "seconds": time.perf_counter() - t0, "info": info, "threads": threads})
+    return out
+
+
 def bench_serving(args, seconds=10.0, drain_s=20.0):
     """Poisson 200 req/s, n log-uniform [64, 32768] + 1% n=131072, 30% repeats;
     mixed form beside the plain FP64 form; plus a sustainable-rate run of the same mix
@@ -906,6 +930,7 @@ def bench_serving(args, seconds=10.0, drain_s=20.0):
     out["fp64"]["note"] = "plain FP64 form on the first fifth of the same trace (it saturates at once)"
     light = make_trace(20, seconds, args.seed + 1, big_frac=0.0)
     out["sustainable_mixed_20req_s"] = run_trace(light, "bf16x3", drain_s)
+    out["cpu_single_request"] = cpu_request_times()
     return out
 
 

@@ -8,7 +8,8 @@
 * the served request trace: arrival rate, repeat share, order distribution, repeats
   naming earlier matrices, determinism;
 * the clock record taken during the timed region: median SM clock, maximum, and the
-  throttle reasons a measurement is judged by.
+  throttle reasons a measurement is judged by;
+* the CPU path's single-request times that the serving report carries.
 """
 import json
 import math
@@ -153,3 +154,11 @@ def test_clock_record_thermal(tmp_path):
 def test_clock_record_empty(tmp_path):
     c = _record(tmp_path, [])
     assert c["sm_mhz"] is None and c["reasons"] == ["no samples"]
+
+
+# ---------------------------------------------------------------- CPU single-request times
+def test_cpu_request_times(oracle_mod):
+    rows = bench.cpu_request_times(sizes=(64, 200), threads=2)
+    assert [r["n"] for r in rows] == [64, 200]
+    for r in rows:
+        assert r["info"] == 0 and r["seconds"] > 0 and r["nb"] <= r["n"] and r["threads"] == 2
