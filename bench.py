@@ -679,7 +679,8 @@ def run_mixed(args):
             "config": {"workload": _workload_name(args), "form": "mixed", "n": n, "nb": nb, "prec": args.prec,
                        "delta": args.delta, "nrhs": nrhs, "parallelism": f"replicas x{world}",
                        "l2": f"inputs larger than L2 ({n * n * 8 / 1e9:.1f} GB)"},
-            "refinement": {"iterations": iters, "backward_error": max(berrs)},
+            "refinement": {"iterations": iters, "backward_error": max(berrs),
+                           "solves_per_s": world * 1e3 / ms if ms > 0 else None},
             "fp64": fp64, "errors": errors,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
             "factor_seconds_avg": fac_s / args.steps,
