@@ -8,9 +8,9 @@ One JSON line on rank 0.  Two forms (``--form``):
   column solves and trailing updates) followed by FP64 iterative refinement to a normwise
   backward error <= 1e-14.  ``value`` = n^3/3 / step time with A resident in HBM;
   ``fp64`` = the same solve done by the plain FP64 path, measured once; the forward and
-  backward errors of every solve are reported per delta.  The plain FP64 out-of-core case at n=163840
-  (214.7 GB pinned host matrix) does not fit the host RAM of these boxes (209 GB in
-  total) and is not run.
+  backward errors of every solve are reported per delta.  The plain FP64 out-of-core
+  case at n=163840 (214.7 GB pinned host matrix) does not fit the host RAM of these
+  boxes (209 GB in total) and is not run.
 * ``fp64-ooc``: the plain FP64 out-of-core factorization at n=24576 with the 1024-wide
   tiles of the n=163840 case and a 1 GiB device budget for the host leg.
 
