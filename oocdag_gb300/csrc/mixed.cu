@@ -1,16 +1,22 @@
 // Mixed-precision factorization and FP64 solves with iterative refinement.
 //
-// The factorization keeps the structure of the plain path (diagonal-tile potrf in FP64,
-// then the column solve, oocquark.cpp:393-410 in the reference; the column solve is a
-// product with the tile's FP64 inverse, in FP32 for a reduced-precision factor) but runs
-// the trailing syrk/gemm updates (oocquark.cpp:346,351) in reduced precision:
-//   OOC_PREC_FP32  : FP32 copies of the column panel, FP32 FFMA products accumulated in
-//                    FP32, subtracted from the FP64 trailing matrix;
-//   OOC_PREC_BF16X3: hi/lo BF16 splits of the column panel, three tensor-core products
-//                    (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM (tc_bf16x3.cu).
-// The factor is then used for a solve whose residuals are computed in FP64 against the
-// untouched FP64 matrix, refining the solution until the normwise backward error
-// ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches the requested tolerance.
+// Factor objects.  OOC_PREC_FP64 is the plain path's right-looking factorization (device
+// potrf, inverse-based column solve and DMMA updates).  The reduced precisions keep the
+// reference's per-panel structure (diagonal-tile potrf, column solve, trailing syrk/gemm:
+// oocquark.cpp:393-410, 346, 351) on an FP32 working matrix that becomes the factor:
+//   diagonal tile  : FP32 Cholesky and inverse in one CTA (k_diag_s256 for tiles of up to
+//                    256 columns, held in shared memory; k_diag_f32 for wider ones);
+//   column solve   : the panel times the tile's inverse, in FP32 (k_colsolve_f32) or as
+//                    three split-BF16 tensor-core products (k_trsm2_bf16x3, tc_bf16x3.cu);
+//   trailing update: OOC_PREC_FP32 - FP32 FFMA products (k_syrk_f32);
+//                    OOC_PREC_BF16X3 - hi/lo BF16 planes of the panel, three tensor-core
+//                    products (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM and added
+//                    into the FP32 trailing matrix by TMA reductions (k_syrk2_bf16x3).
+// Split-BF16 factors use nb/2-wide panels for the last OOC_OPT_TAIL_ORDER orders.
+// Solves use the kept inverses of the diagonal tiles (solve_with).  The refinement
+// computes residuals in FP64 against the FP64 matrix (device, or the lower triangle of a
+// host matrix copied once), and corrects with the FP32 factor until the normwise backward
+// error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches the tolerance.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -26,7 +32,7 @@
 namespace {
 
 // ---------------------------------------------------------------------------------
-// FP32 lower-triangular rank-K update: C (FP64, lower) -= X X^T with X (m x K, FP32,
+// FP32 lower-triangular rank-K update: C (FP32 or FP64, lower) -= X X^T with X (m x K, FP32,
 // column-major, ld ldx).  128 x 128 output blocks, lower-triangular block grid.
 // ---------------------------------------------------------------------------------
 constexpr int FB = 128, FK = 16, FTHR = 256;
