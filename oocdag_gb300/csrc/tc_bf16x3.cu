@@ -1,4 +1,13 @@
-// Split-BF16 tensor-core trailing update on Blackwell (tcgen05 + TMA + TMEM).
+// Split-BF16 tensor-core kernels on Blackwell (tcgen05 + TMA + TMEM) for the mixed path:
+//   k_split_bf16        hi/lo BF16 planes of a column panel (K-major);
+//   k_syrk_bf16x3<TC>   trailing update C (lower) -= X X^T in 128 x 128 blocks with a
+//                       read-modify-write epilogue: FP64 C, and FP32 C whose base or
+//                       leading dimension is not 16-byte aligned;
+//   k_syrk2_bf16x3<TC>  the same for 16-byte-aligned FP32 C (the working matrix of
+//                       reduced-precision factors) in 256 x 128 blocks, C updated by TMA
+//                       reductions, blocks taken from a run-time ticket counter;
+//   k_trsm2_bf16x3      the column solve P = U X^T with the same three products.
+// Each kernel's own comment gives its layout; the 128 x 128 update is described here.
 //
 //   C (FP64, lower triangle) -= X X^T,   X = m x K (FP64, column-major)
 //
