@@ -4,9 +4,10 @@
 // each would be a handful of tiny launches.  Here every CTA of a persistent grid takes
 // the next matrix from a queue sorted by decreasing size (largest first balances the
 // tail), factors it with a blocked right-looking Cholesky inside the CTA (diagonal block
-// in shared memory, panel solve thread-per-row, trailing update from a shared-memory
-// copy of the panel with 4 x 4 register tiles), then solves for its right-hand side,
-// and moves on.  Per-matrix LAPACK info goes to an array; a failed matrix is skipped.
+// in shared memory, factored by one warp in registers for FP32 and column by column by
+// the CTA for FP64; panel solve thread-per-row with the row in registers; trailing update
+// from a shared-memory copy of the panel with 4 x 4 register tiles), then solves for its
+// right-hand side, and moves on.  Per-matrix LAPACK info goes to an array; a failed matrix is skipped.
 // The panel width is chosen per size bucket by the autotuner (oocdag_gb300/autotune.py).
 //
 // The per-tile arithmetic restates the reference's task bodies at small n: the
