@@ -696,7 +696,7 @@ def run_mixed(args):
 
 
 # ----------------------------------------------------------------------------------
-# batched small systems (20,000, n in [16, 512]) in one persistent launch
+# launch and flop accounting from the factor's schedule
 # ----------------------------------------------------------------------------------
 def refine_launches(iters, npanels):
     """Kernels one ooc_solve_refine call launches on an FP32 or split-BF16 factor (device
@@ -725,6 +725,9 @@ def panel_schedule(n, nb, prec, tail_order):
     return out
 
 
+# ----------------------------------------------------------------------------------
+# batched small systems (20,000, n in [16, 512]) in one persistent launch
+# ----------------------------------------------------------------------------------
 def bench_batched(h, args, count=20000, reps=3):
     """20000 SPD systems, n ~ U{16..512}, A = M M^T/n + I (M ~ N(0,1)), one N(0,1) RHS each,
     FP64 and FP32; tile widths from the autotuner; results compared per matrix with the
