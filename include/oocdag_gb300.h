@@ -267,10 +267,14 @@ int ooc_server_destroy(ooc_server* s);
  * NULL = the legacy default stream).  A: host (pageable or page-locked) or device,
  * column-major, lower triangle factored in place as ooc_dpotrf_L does.
  * - Limit: the matrix must fit the reference's panel rule in OOC_STATIC_PANEL_BYTES with
- *   one X buffer (about 2*ceil(n/nb)+1 tiles of nb*nb doubles); larger sizes return
- *   OOC_ERR_BUDGET with a message in ooc_last_error_string().
+ *   one X buffer: at least 2*ceil(n/nb) tiles of nb*nb doubles (n <= 16384 at nb = 256);
+ *   larger sizes return OOC_ERR_BUDGET, before any device call, with a message in
+ *   ooc_last_error_string().
  * - The first call on a device looks up the array's device address (set-up); make that
- *   first call before any stream capture.
+ *   first call before any stream capture.  The lookup is kept per device context, so it
+ *   runs again after the device or its primary context has been reset.
+ * - The call waits (bounded) until its work on `stream` has finished, then reads the
+ *   status word, so it returns with A factored and *info set.
  * - Calls share the array: the status word is cleared at the start of each call; calls
  *   whose GPU work overlaps (e.g. two threads on two streams) race and must be
  *   serialized by the caller.                                                        */

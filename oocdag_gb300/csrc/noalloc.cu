@@ -14,6 +14,7 @@
 // call; two calls whose work overlaps on the GPU (for example from two host threads on
 // two streams) race on the array and must be serialized by the caller.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,38 +34,75 @@ static_assert(kStaticBytes % 256 == 0, "static panel size must keep 256-byte ali
 static __device__ __align__(256) double g_static_panel[kStaticBytes / sizeof(double)];
 static __device__ __align__(256) int g_static_status[64];
 
-// Device addresses of the arrays above, looked up once per device with that device
-// current.  In host code the array names are host-side stand-ins, never device
-// addresses: only these looked-up pointers are passed to kernels.
+// Device addresses of the arrays above, looked up (set-up) once per device context with
+// that context current.  In host code the array names are host-side stand-ins, never
+// device addresses: only these looked-up pointers are passed to kernels and copies.
+// The cache is keyed by the driver's context ID, not by the device number: when a
+// caller resets the device (cudaDeviceReset, or another library resetting the primary
+// context), the next context loads the module afresh and the arrays may sit at other
+// addresses, so a new context ID means a new lookup.  IDs are never reused within a
+// process.  Without the driver entry points the lookup runs on every call (it
+// allocates nothing).
 struct StaticPtrs {
   double* panel = nullptr;
   int* status = nullptr;
+  unsigned long long ctx_id = 0;
   bool ready = false;
 };
 std::mutex g_mu;
 StaticPtrs g_ptrs[64];
 
+typedef CUresult (*ctx_get_current_t)(CUcontext*);
+typedef CUresult (*ctx_get_id_t)(CUcontext, unsigned long long*);
+ctx_get_current_t g_ctx_current = nullptr;
+ctx_get_id_t g_ctx_id = nullptr;
+std::once_flag g_entry_once;
+
+// ID of the context current on this thread; false if there is none or it is unknown.
+bool current_context_id(unsigned long long* id) {
+  std::call_once(g_entry_once, [] {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+        qa == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+        qb == cudaDriverEntryPointSuccess) {
+      g_ctx_current = (ctx_get_current_t)a;
+      g_ctx_id = (ctx_get_id_t)b;
+    }
+  });
+  if (!g_ctx_current || !g_ctx_id) return false;
+  CUcontext ctx = nullptr;
+  if (g_ctx_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+  return g_ctx_id(ctx, id) == CUDA_SUCCESS;
+}
+
 int static_setup(int dev, StaticPtrs* out) {
   if (dev < 0 || dev >= 64) return OOC_ERR_NODEVICE;
   std::lock_guard<std::mutex> lk(g_mu);
   StaticPtrs& p = g_ptrs[dev];
-  if (!p.ready) {
-    void* a = nullptr;
-    void* b = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&a, g_static_panel);
-    if (e != cudaSuccess) {
-      ooc_set_last_error(e, "cudaGetSymbolAddress(g_static_panel)", __FILE__, __LINE__);
-      return OOC_ERR_CUDA;
-    }
-    e = cudaGetSymbolAddress(&b, g_static_status);
-    if (e != cudaSuccess) {
-      ooc_set_last_error(e, "cudaGetSymbolAddress(g_static_status)", __FILE__, __LINE__);
-      return OOC_ERR_CUDA;
-    }
-    p.panel = (double*)a;
-    p.status = (int*)b;
-    p.ready = true;
+  unsigned long long id = 0;
+  if (p.ready && current_context_id(&id) && id == p.ctx_id) {
+    *out = p;
+    return OOC_OK;
   }
+  p.ready = false;
+  void* a = nullptr;
+  void* b = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&a, g_static_panel);  // also initialises the context
+  if (e != cudaSuccess) {
+    ooc_set_last_error(e, "cudaGetSymbolAddress(g_static_panel)", __FILE__, __LINE__);
+    return OOC_ERR_CUDA;
+  }
+  e = cudaGetSymbolAddress(&b, g_static_status);
+  if (e != cudaSuccess) {
+    ooc_set_last_error(e, "cudaGetSymbolAddress(g_static_status)", __FILE__, __LINE__);
+    return OOC_ERR_CUDA;
+  }
+  p.panel = (double*)a;
+  p.status = (int*)b;
+  p.ready = current_context_id(&p.ctx_id);  // cached only when the context is known
   *out = p;
   return OOC_OK;
 }
@@ -132,22 +170,27 @@ int update_split(const TileCol& X, const TileMap& C, int Ht, int Kt, i64 H, i64 
     }                                                        \
   } while (0)
 
+// The panel rule with one X buffer needs at least 2 * ceil(n/nb) tiles for the first
+// panel (oocdag.cpp:483-486 with Yn = 1: (memBlock - Ym) * 2 >= 2 * Ym).  Host only.
+int check_fits(i64 n, int nb) {
+  const i64 bb = (n + nb - 1) / nb;
+  const i64 memBlock = (i64)(kStaticBytes / sizeof(double) / ((size_t)nb * (size_t)nb));
+  if (memBlock < 2 * bb) {
+    char buf[256];
+    snprintf(buf, sizeof(buf),
+             "ooc_dpotrf_L_static: n=%lld with nb=%d needs more than the %zu-byte static panel buffer "
+             "(%lld tiles of %d x %d available, at least %lld needed)",
+             (long long)n, nb, kStaticBytes, (long long)memBlock, nb, nb, 2LL * bb);
+    ooc_set_last_message(buf);
+    return OOC_ERR_BUDGET;
+  }
+  return OOC_OK;
+}
+
 int run_static(double* A, i64 n, i64 lda, int nb, cudaStream_t s, const StaticPtrs& P, int* info) {
   const int bb = (int)((n + nb - 1) / nb);
   const i64 tile = (i64)nb * nb;
   const i64 memBlock = (i64)(kStaticBytes / sizeof(double) / (size_t)tile);
-  {
-    int st = 0;
-    if (memBlock <= 0 || width_one_x(bb, memBlock, 0, &st) <= 0) {
-      char buf[256];
-      snprintf(buf, sizeof(buf),
-               "ooc_dpotrf_L_static: n=%lld with nb=%d needs more than the %zu-byte static panel buffer "
-               "(%lld tiles of %d x %d available, at least %d needed)",
-               (long long)n, nb, kStaticBytes, (long long)memBlock, nb, nb, 2 * bb + 1);
-      ooc_set_last_message(buf);
-      return OOC_ERR_BUDGET;
-    }
-  }
   double* Y = P.panel;
   int* status = P.status;
   NA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));  // the shared word keeps the last call's value
@@ -211,9 +254,14 @@ int run_static(double* A, i64 n, i64 lda, int nb, cudaStream_t s, const StaticPt
     JB += YN;
     jb += Yn;
   }
+  // Wait (bounded) for the stream, then read the status word.  The host word is pageable
+  // stack memory, so the copy returns only once it is done; with the stream idle it
+  // finishes at once and never waits without bound.
+  int rc = wait_stream_bounded(s, 6LL * 3600 * 1000);
+  if (rc) return rc;
   int host_status = 0;
   NA_TRY(cudaMemcpyAsync(&host_status, status, sizeof(int), cudaMemcpyDeviceToHost, s));
-  int rc = wait_stream_bounded(s, 6LL * 3600 * 1000);
+  rc = wait_stream_bounded(s, 60LL * 1000);
   if (rc) return rc;
   *info = host_status;
   return OOC_OK;
@@ -229,6 +277,8 @@ extern "C" int ooc_dpotrf_L_static(double* A, int64_t n, int64_t lda, int nb, vo
   if (!info) return -6;
   *info = 0;
   if (n == 0) return OOC_OK;
+  int rc = check_fits(n, nb);  // host arithmetic only: no device call before it
+  if (rc) return rc;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -236,7 +286,7 @@ extern "C" int ooc_dpotrf_L_static(double* A, int64_t n, int64_t lda, int nb, vo
     return OOC_ERR_NODEVICE;
   }
   StaticPtrs P;
-  int rc = static_setup(dev, &P);
+  rc = static_setup(dev, &P);
   if (rc) return rc;
   return run_static(A, n, lda, nb, (cudaStream_t)stream, P, info);
 }

@@ -5,11 +5,14 @@ use this package, and only to check or time the GPU library: the product never
 imports it.  The C++ restatement lives in ``ooc_oracle.cpp``; this module builds it
 (``build()``), loads it with ctypes and wraps it for numpy arrays.
 
-Parity status: the reference (efdazedo/oocdag) cannot be built here (MPI, Intel MKL
-with BLACS/ScaLAPACK, QUARK and Fortran are absent).  The oracle is pinned to the
-literal-loop restatements of the reference's generator and panel sizing stored in
-``tests/golden`` and to LAPACK ``dpotrf``; the tile arithmetic itself is the host
-BLAS (SciPy's OpenBLAS) standing in for the reference's MKL/cuBLAS calls.
+Parity status: pinned to the reference's own code.  ``ref_build.py`` compiles the
+reference's ``oocdag.cpp`` and ``oocquark.cpp`` unmodified into ``oracle/_ref`` with host
+stand-ins for its absent dependencies (QUARK in program order, cuBLAS v2 and MKL
+``dpotrf_`` on SciPy's OpenBLAS); ``tests/test_ref_build.py`` shows the oracle's factor
+equal to the compiled reference's bit for bit and its panel plans and task counts equal.
+The generator is pinned to the literal-loop restatement of ``LIN/pdmatgen.f`` in
+``tests/golden`` (the reference's Fortran is not compiled: no Fortran compiler), and the
+tile arithmetic is host BLAS standing in for the reference's MKL/cuBLAS calls.
 """
 from __future__ import annotations
 

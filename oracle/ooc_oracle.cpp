@@ -5,13 +5,13 @@
 // it.  Only tests, the smoke check and the CPU-baseline leg of the benchmark may load
 // it; the GPU product never links, calls or falls back to it.
 //
-// Parity status: the reference cannot be built here (it needs MPI, Intel MKL with
-// BLACS/ScaLAPACK, the QUARK runtime and a Fortran compiler).  The restatement is
-// pinned (a) to literal-loop restatements of the reference's generator and panel
-// sizing (tests/golden), (b) to a program-order execution of the same task list, and
-// (c) to LAPACK dpotrf on the same matrices.  Tile arithmetic is delegated to host
-// BLAS/LAPACK (OpenBLAS bundled with SciPy), standing in for the MKL and cuBLAS calls
-// the reference makes at oocquark.cpp:87,130,176,222.
+// Parity status: pinned (a) to the reference's own oocdag.cpp/oocquark.cpp compiled
+// unmodified with host stand-ins for QUARK, cuBLAS and MKL (oracle/ref_build.py,
+// oracle/_ref): this oracle's factor equals that build's bit for bit, and its panel
+// plans and task counts equal the reference's; (b) to a literal-loop restatement of the
+// reference's Fortran generator (tests/golden); (c) to LAPACK dpotrf.  Tile arithmetic
+// is delegated to host BLAS/LAPACK (OpenBLAS bundled with SciPy), standing in for the
+// MKL and cuBLAS calls the reference makes at oocquark.cpp:87,130,176,222.
 //
 // What follows the reference (paths relative to the reference project):
 //   orc_find_Yn          oocdag.cpp:478-492  (the function-local `static Yn` becomes

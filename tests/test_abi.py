@@ -131,3 +131,20 @@ def test_factor_bytes_accounting(ooc):
         assert b64 >= 8 * n * n
     assert L.ooc_factor_bytes(65536, 512, ooc.PREC_BF16X3) < 18 * 10 ** 9  # fits beside A in 280 GB
     assert L.ooc_factor_bytes(0, 512, ooc.PREC_FP64) == 0 and L.ooc_factor_bytes(16, 0, ooc.PREC_FP64) == 0
+
+
+def test_static_entry_size_limit_needs_no_gpu(ooc):
+    """ooc_dpotrf_L_static checks the size against its 64 MiB array before any device call:
+    the first panel needs 2*ceil(n/nb) tiles, so at nb=256 (128 tiles of 512 KiB) n=16384
+    (64 tile columns) passes the check and n=16385 (65) is rejected."""
+    L = ooc.load()
+    info = ctypes.c_int(-1)
+    dummy = (ctypes.c_double * 1)()
+    rc = L.ooc_dpotrf_L_static(dummy, 16385, 16385, 256, None, ctypes.byref(info))
+    assert rc == ooc.OOC_ERR_BUDGET
+    msg = L.ooc_last_error_string()
+    assert b"128 tiles" in msg and b"at least 130 needed" in msg, msg
+    if not gpu_available():
+        # past the size check the call needs a device, and says so
+        rc = L.ooc_dpotrf_L_static(dummy, 16384, 16384, 256, None, ctypes.byref(info))
+        assert rc == ooc.OOC_ERR_NODEVICE

@@ -91,6 +91,54 @@ def test_ooc_host_matches_oracle_and_is_schedule_invariant(oracle_mod, handle, o
     np.testing.assert_array_equal(np.triu(results[0][1], 1), np.triu(A, 1))
 
 
+def test_ooc_matches_compiled_reference_fixture(oracle_mod, handle, ooc):
+    """The library's factor against the reference's own output (tests/golden/ref_run.npz,
+    made by the reference's oocdag.cpp/oocquark.cpp compiled unmodified), with the
+    reference's panel schedule (one X buffer, its budget) and the library's default."""
+    import os
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_run.npz"))
+    names = [k for k in z.files if not k.endswith("_meta")]
+    assert len(names) >= 3
+    for name in names:
+        n, nb, tiles, kind, seed, npanels = (int(v) for v in z[name + "_meta"])
+        A = oracle_mod.gen_uniform(n, seed, float(n)) if kind == 0 else oracle_mod.gen_pdmatgen(n, seed)
+        Lref = np.zeros((n, n))
+        Lref[np.tril_indices(n)] = z[name]
+        for ref_schedule in (1, 0):
+            handle.set_option(ooc.OPT_REF_SCHEDULE, ref_schedule)
+            handle.set_option(ooc.OPT_X_BUFFERS, 1 if ref_schedule else 2)
+            try:
+                H = A.copy(order="F")
+                r = handle.dpotrf_L(H, n, n, nb, tiles * nb * nb * 8)
+            finally:
+                handle.set_option(ooc.OPT_REF_SCHEDULE, 0)
+                handle.set_option(ooc.OPT_X_BUFFERS, 2)
+            assert r.info == 0
+            if ref_schedule:
+                assert r.stats["npanels"] == npanels, name
+            np.testing.assert_allclose(np.tril(H), Lref, rtol=0, atol=ATOL_REL * np.abs(Lref).max(), err_msg=name)
+            np.testing.assert_array_equal(np.triu(H, 1), np.triu(A, 1))
+            k = "uniform" if kind == 0 else "pdmatgen"
+            alpha = float(n) if kind == 0 else 0.0
+            rg = oracle_mod.residual(H, k, seed, alpha, tile=64)
+            rr = oracle_mod.residual(np.asfortranarray(Lref), k, seed, alpha, tile=64)
+            assert rg <= RESID_RATIO * rr and rr <= RESID_RATIO * rg, (name, rg, rr)
+
+
+def test_ooc_wide_tiles_several_panels(oracle_mod, handle):
+    """nb=1024 (the largest configuration's tile) streamed through a budget that forces at
+    least three panels, against the oracle at the same tile width."""
+    n, nb, tiles = 5120, 1024, 15  # three panels: (0,5,1), (1,4,2), (3,2,2)
+    A = oracle_mod.gen_uniform(n, 100, float(n))
+    Lo, info_o = _oracle_factor(oracle_mod, A, nb, tiles)
+    H = A.copy(order="F")
+    r = handle.dpotrf_L(H, n, n, nb, tiles * nb * nb * 8)
+    assert r.info == 0 == info_o and r.stats["npanels"] >= 3, r.stats
+    _check_parity(oracle_mod, H, Lo, "uniform", 100, float(n))
+    np.testing.assert_array_equal(np.triu(H, 1), np.triu(A, 1))
+
+
 def test_config0_in_core_host(oracle_mod, handle):
     # n=4096, nb=256, 24 GB budget: one panel through host memory.
     n, nb = 4096, 256

@@ -282,3 +282,37 @@ def test_pooled_buffers_give_identical_factors(oracle_mod, handle, ooc):
         handle.set_option(ooc.OPT_POOL_BYTES, cap)
     for L in again + [fresh]:
         np.testing.assert_array_equal(L, first)
+
+
+@pytest.mark.parametrize("tail", [24576, 8192])
+def test_split_bf16_at_bench_tile_width_n16384(oracle_mod, handle, ooc, tail):
+    # The benchmark's tile width (nb=512) at n=16384: the default tail schedule (every
+    # panel 256 wide here, diagonal tiles in shared memory) and a switch at order 8192
+    # (512-wide panels and their diagonal kernel first).  The trailing updates run the
+    # persistent 256x128 tcgen05 kernel up to m ~ 16k.  Against the oracle's FP64 solve.
+    import os
+
+    import torch
+
+    n, nb = 16384, 512
+    A, alpha = _c2_matrix(oracle_mod, n, 0.1)
+    B = np.asfortranarray(np.random.default_rng(16).standard_normal((n, 1)))
+    Lo = A.copy(order="F")
+    _, info_o, _ = oracle_mod.cholesky(Lo, nb, 8 << 30, max(4, (os.cpu_count() or 8) - 2), 2)
+    assert info_o == 0
+    Xo = oracle_mod.potrs(Lo, B)
+    del Lo
+    Ad, Bd = _dev(A), _dev(B)
+    Xd = torch.empty_like(Bd)
+    handle.set_option(ooc.OPT_TAIL_ORDER, tail)
+    try:
+        with handle.factor(Ad, n, n, nb, "bf16x3") as F:
+            assert F.info == 0
+            it, be = F.refine(Ad, n, Bd, n, Xd, n, 1, BERR_TOL, 30)
+    finally:
+        handle.set_option(ooc.OPT_TAIL_ORDER, 24576)
+    X = _host(Xd)
+    assert be <= BERR_TOL and 1 <= it <= 5, (it, be)
+    assert _berr(A, X, B) <= 2 * BERR_TOL
+    fwd = np.abs(X - Xo).max() / np.abs(Xo).max()
+    assert fwd < FWD_TOL, fwd

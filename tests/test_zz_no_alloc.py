@@ -67,3 +67,49 @@ def test_static_entry_rejects_sizes_beyond_its_array(ooc, handle):
     rc = L.ooc_dpotrf_L_static(ctypes.c_void_p(A.ctypes.data), n, n, nb, None, ctypes.byref(info))
     assert rc == ooc.OOC_ERR_BUDGET
     assert b"static panel buffer" in L.ooc_last_error_string()
+
+
+def test_static_entry_device_matrix_on_a_caller_stream(oracle_mod, ooc, handle):
+    """A already in device memory (a torch tensor: the copies become device-to-device) on a
+    stream the caller created, then a failing matrix on the device that stops early."""
+    import torch
+
+    L = ooc.load()
+    n, nb = 2500, 256
+    A = oracle_mod.gen_uniform(n, 9, float(n))
+    ref = A.copy(order="F")
+    assert handle.dpotrf_L(ref, n, n, nb, 64 << 20).info == 0
+    s = torch.cuda.Stream()
+    T = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()  # row-major (n, n) == column-major A
+    torch.cuda.synchronize()
+    info = ctypes.c_int(-1)
+    rc = L.ooc_dpotrf_L_static(ctypes.c_void_p(T.data_ptr()), n, n, nb, ctypes.c_void_p(s.cuda_stream),
+                               ctypes.byref(info))
+    assert rc == 0, L.ooc_last_error_string()
+    assert info.value == 0
+    got = np.asfortranarray(T.cpu().numpy().T)
+    Lr = np.tril(ref)
+    np.testing.assert_allclose(np.tril(got), Lr, rtol=0, atol=ATOL_REL * np.abs(Lr).max())
+    np.testing.assert_array_equal(np.triu(got, 1), np.triu(A, 1))
+    bad = A.copy(order="F")
+    bad[1900, 1900] = -4.0
+    Tb = torch.from_numpy(np.ascontiguousarray(bad.T)).cuda()
+    torch.cuda.synchronize()
+    rc = L.ooc_dpotrf_L_static(ctypes.c_void_p(Tb.data_ptr()), n, n, nb, ctypes.c_void_p(s.cuda_stream),
+                               ctypes.byref(info))
+    assert rc == 0 and info.value == 1901
+
+
+def test_static_entry_at_its_largest_order(oracle_mod, ooc, handle):
+    # n=16384 at nb=256 needs exactly the array's 128 tiles for its first panel
+    L = ooc.load()
+    n, nb = 16384, 256
+    A = oracle_mod.gen_uniform(n, 12, float(n))
+    got = A.copy(order="F")
+    rc, info = _static_call(L, got, n, n, nb)
+    assert rc == 0, L.ooc_last_error_string()
+    assert info == 0
+    ref = A.copy(order="F")
+    assert handle.dpotrf_L(ref, n, n, nb, 1 << 30).info == 0
+    Lr = np.tril(ref)
+    np.testing.assert_allclose(np.tril(got), Lr, rtol=0, atol=ATOL_REL * np.abs(Lr).max())
