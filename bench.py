@@ -68,6 +68,10 @@ def parse():
     p.add_argument("--no-fp64-ref", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the batched small-system and served request-stream runs")
+    p.add_argument("--block-cols", type=int, default=None,
+                   help="OOC_OPT_BLOCK_COLS for the device-resident leg (default: the library's choice)")
+    p.add_argument("--errors-n", type=int, default=16384,
+                   help="order of the per-delta forward-error table (each against a plain FP64 solve)")
     a = p.parse_args()
     if a.n is None:
         a.n = 65536 if a.form == "mixed" else 24576
@@ -428,6 +432,34 @@ def _measured_peaks() -> dict:
         return {}
 
 
+def link_probe(nbytes: int = 2 << 30, reps: int = 4) -> dict:
+    """Page-locked host<->device copy rate on this machine (one copy engine per direction,
+    CUDA events, best of `reps` after one warm-up): the peak the e2e copies are held to."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    h.fill_(1)
+    s = torch.cuda.Stream()
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = 0.0
+        for r in range(reps + 1):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                e0.record(s)
+                dst.copy_(src, non_blocking=True)
+                e1.record(s)
+            e1.synchronize()
+            if r:
+                best = max(best, nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9)
+        out[name] = best
+    out["bytes"] = nbytes
+    del h, d
+    return out
+
+
 def run_mixed(args):
     """Mixed factor + FP64 refinement, with the plain FP64 solve beside it."""
     rank, world, local = _init_dist()
@@ -442,10 +474,13 @@ def run_mixed(args):
     flops = n ** 3 / 3.0
     alpha = lambda d: 0.5774 * (n ** 0.5) * (1 + d)
     h = ooc.Handle(local)
+    if args.block_cols is not None:
+        h.set_option(ooc.OPT_BLOCK_COLS, args.block_cols)
     comp = torch.cuda.ExternalStream(h.stream(0))
     peaks = _measured_peaks()
     hbm_peak = peaks.get("hbm_gbs")
     fp64_peak = h.fp64_peak(300.0)
+    link = link_probe()
 
     A = torch.empty((n, n), dtype=torch.float64, device="cuda")  # column-major, ld = n
     h.matgen_uniform(A, n, n, seed, alpha(args.delta))
@@ -466,7 +501,8 @@ def run_mixed(args):
 
     for _ in range(args.warmup):
         solve(args.prec)
-    npanels = len(panel_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER)))
+    npanels = len(update_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER),
+                                  h.get_option(ooc.OPT_BLOCK_COLS))["panels"])
     h.set_option(ooc.OPT_PROFILE, 1)
     clocks = ClockSampler(local)
     clocks.start()
@@ -529,6 +565,9 @@ def run_mixed(args):
         if Ad is not A:
             del Ad
     torch.cuda.empty_cache()
+    # forward errors of every delta and nrhs against the plain FP64 solve of the same system,
+    # at an order where the FP64 factorization takes seconds
+    errors_small = forward_error_table(h, args, seed) if args.errors_n else None
 
     # ---- e2e: host A and b through the C-ABI ------------------------------------------
     # The factor takes the pinned host matrix itself: it copies the lower triangle (the
@@ -543,9 +582,16 @@ def run_mixed(args):
         Xh = torch.empty_like(Bh)
         Bd = torch.empty((nrhs, n), dtype=torch.float64, device="cuda")
         Xd = torch.empty_like(Bd)
-        # host-to-device bytes of the lower triangle, column blocks as the library copies them
+        # host-to-device bytes of the lower triangle, in the column chunks the library copies
+        # (rows c0..n-1 of each chunk; chunks of at most 256 MB of column height, and within
+        # one panel of the left-looking schedule)
         wblk = max(1, min(n, (256 << 20) // (8 * n)))
-        a_h2d = sum((n - c0) * min(wblk, n - c0) * 8 for c0 in range(0, n, wblk))
+        hs = update_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER), h.get_option(ooc.OPT_BLOCK_COLS))
+        if hs["kind"] == "right-looking":
+            a_h2d = sum((n - c0) * min(wblk, n - c0) * 8 for c0 in range(0, n, wblk))
+        else:
+            a_h2d = sum((n - c0) * min(wblk, J0 + LN - c0) * 8 for J0, LN in hs["panels"]
+                        for c0 in range(J0, J0 + LN, wblk))
 
         phase = {"h2d_b_ms": 0.0, "factor_incl_a_h2d_ms": 0.0, "refine_ms": 0.0, "close_ms": 0.0, "d2h_ms": 0.0}
 
@@ -582,28 +628,28 @@ def run_mixed(args):
         torch.cuda.synchronize()
         e_ms = allreduce_max(s0.elapsed_time(s1) / args.steps, world)
         h.set_option(ooc.OPT_KEEP_A, 0)
+        bc = h.get_option(ooc.OPT_BLOCK_COLS)
         e2e = {"value": flops * world / (e_ms / 1e3) / 1e12, "unit": "TFLOP/s", "ms_per_step": e_ms,
                "h2d_bytes_per_step": int(a_h2d + nrhs * n * 8), "d2h_bytes_per_step": int(nrhs * n * 8),
-               "path": "ooc_factor_create + ooc_solve_refine on the pinned host matrix (lower triangle copied "
-                       "once, kept for the refinement: OOC_OPT_KEEP_A)",
+               "path": "ooc_factor_create + ooc_solve_refine on the pinned host matrix: the lower triangle "
+                       f"streamed ({hs['kind']}) while earlier blocks are factored, kept for the refinement "
+                       "(OOC_OPT_KEEP_A)",
+               "host_link": link,
+               "copy_time_at_link_peak_ms": a_h2d / (link["h2d_gbs"] * 1e9) * 1e3,
+               "lower_bound_ms": max(ms_local, a_h2d / (link["h2d_gbs"] * 1e9) * 1e3),
                "phases_ms_host_clock": {k: round(v, 2) for k, v in phase.items()}}
         del Ah, Bh, Xh, Bd, Xd
 
     # ---- roofline of the dominant kernel ------------------------------------------------
-    # Trailing update of panel j (m = n - (j+1) nb rows below it, K = nb): algorithmic
-    # m (m+1) K useful flops, three BF16 tensor products of each (hi*hi, hi*lo, lo*hi); bytes:
-    # the FP32 lower triangle read and written (8 B per element), the FP32 panel read by the
-    # split (4 B per element) and the two BF16 planes written and read once (8 B per element).
-    upd_bytes = kern_bytes = 0.0
-    panels = panel_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER))
-    for J0, LN in panels:
-        m = n - J0 - LN
-        if m <= 0:
-            continue
-        upd_bytes += m * (m + 1) / 2 * 8 + m * LN * (4 + 8)
-        kern_bytes += m * (m + 1) / 2 * 8 + m * LN * 4  # what the tcgen05 kernel itself moves
-    upd_bytes *= args.steps
-    kern_bytes *= args.steps
+    # Every trailing-update launch of the factor's schedule (update_schedule): an update of
+    # an m-row trailing matrix restricted to its first `cols` columns with K columns of
+    # finished panels has 2 K lower_elems(m, cols) algorithmic flops (m (m+1) K for a whole
+    # trailing matrix) and moves the FP32 lower part of C in and out once per launch (8 B
+    # per element) plus the BF16 hi/lo planes of X once (4 B per element of the m x K panel).
+    sched = update_schedule(n, nb, args.prec, h.get_option(ooc.OPT_TAIL_ORDER), h.get_option(ooc.OPT_BLOCK_COLS))
+    panels = sched["panels"]
+    kern_bytes = sum(8 * lower_elems(m, cols) + 4 * m * K for m, K, cols in sched["launches"]) * args.steps
+    upd_bytes = kern_bytes
     share_upd = upd_ms / (ms_local * args.steps)
     share_fac = fac_ms / (ms_local * args.steps)
     bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
@@ -612,23 +658,32 @@ def run_mixed(args):
                           "FP32 C updated by TMA reductions)"
                 if args.prec == "bf16x3" else "k_syrk_f32<float> (FP32 FFMA trailing update)",
                 "bound": "tensor" if args.prec == "bf16x3" else "fp32-simt",
-                "achieved": mult * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
+                "achieved": upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
                 "peak": bf16_peak if args.prec == "bf16x3" else None, "unit": "TFLOP/s",
+                "flops_convention": "algorithmic: 2 K per lower-triangle output element (m(m+1)K for a whole "
+                                    "trailing matrix), the Cholesky's own flops",
                 "launches": upd_launch, "avg_launch_ms": upd_ms / max(1, upd_launch), "share_of_step": share_upd,
-                "algorithmic_flops_per_launch": mult * upd_flops / max(1, upd_launch),
+                "launch_unit": "one timed update segment: a panel's narrow + bulk launches, or one block catch-up "
+                               "(its K-chunk launches)",
+                "algorithmic_flops_per_launch": upd_flops / max(1, upd_launch),
+                "tensor_products": mult,
+                "tensor_pipe_achieved": mult * upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
                 "dram_gbs_algorithmic": upd_bytes / (upd_ms / 1e3) / 1e9 if upd_ms else None,
                 "hbm_peak_gbs": hbm_peak,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured; the kernel runs inside a "
                                "seconds-long step)"}
     if upd_roof["achieved"] and upd_roof["peak"]:
         upd_roof["frac"] = upd_roof["achieved"] / upd_roof["peak"]
+        upd_roof["tensor_pipe_frac"] = upd_roof["tensor_pipe_achieved"] / upd_roof["peak"]
     if args.prec == "bf16x3" and upd_launch:
         # DRAM bytes per launch: the algorithmic kernel bytes scaled by the measured/algorithmic
         # ratio of one ncu capture (bulk update at n=16384 with 512-wide panels, m=15872, block columns 4..:
         # 967.5 MB measured, 976.3 MB algorithmic)
         upd_roof["traffic"] = UPDATE_TRAFFIC_RATIO * kern_bytes / upd_launch
-        upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one bulk-update launch "
-                                      "(kernel_bench mixed --n 16384 --nb 512 --tail-order 0), scaled to this workload's launches")
+        upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per algorithmic byte of "
+                                      "update launches captured at n=16384 (profiles/), times this workload's "
+                                      "algorithmic bytes per launch")
+        upd_roof["schedule"] = sched["kind"]
     chain_flops = sum(2 * LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in panels) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_s256 / k_diag_f32 (FP32 potrf + inverse of the 256- / 512-wide "
                           "diagonal tile, one CTA) + "
@@ -681,7 +736,7 @@ def run_mixed(args):
                        "l2": f"inputs larger than L2 ({n * n * 8 / 1e9:.1f} GB)"},
             "refinement": {"iterations": iters, "backward_error": max(berrs),
                            "solves_per_s": world * 1e3 / ms if ms > 0 else None},
-            "fp64": fp64, "errors": errors,
+            "fp64": fp64, "errors": errors, "errors_vs_fp64_solve": errors_small,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
             "factor_seconds_avg": fac_s / args.steps,
             **extra,
@@ -693,6 +748,35 @@ def run_mixed(args):
 
         dist.destroy_process_group()
     return 0
+
+
+def forward_error_table(h, args, seed):
+    """Every delta and nrhs at order args.errors_n: the mixed solve's iterations, backward
+    error and forward error against the plain FP64 solve (FP64 factor + FP64 refinement)
+    of the same system."""
+    import torch
+
+    n, nb = args.errors_n, args.nb
+    A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + 1)
+    B = torch.randn((16, n), dtype=torch.float64, device="cuda", generator=g)
+    X = torch.empty_like(B)
+    X64 = torch.empty_like(B)
+    out = []
+    for d in (1.0, 0.1, 0.01):
+        h.matgen_uniform(A, n, n, seed, 0.5774 * (n ** 0.5) * (1 + d))
+        with h.factor(A, n, n, nb, "fp64") as F64:
+            F64.refine(A, n, B, n, X64, n, 16, 1e-14, 30)
+        with h.factor(A, n, n, nb, args.prec) as F:
+            for r in (1, 16):
+                it, be = F.refine(A, n, B, n, X, n, r, 1e-14, 30)
+                fe = float(((X[:r] - X64[:r]).abs().max() / X64[:r].abs().max()).item())
+                out.append({"n": n, "delta": d, "nrhs": r, "iterations": it, "backward_error": be,
+                            "forward_error_vs_fp64": fe})
+    del A, B, X, X64
+    torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------------------------------
@@ -711,9 +795,9 @@ def refine_launches(iters, npanels):
 
 
 def panel_schedule(n, nb, prec, tail_order):
-    """(J0, width) of the factor's panels, as the library schedules them: nb wide, and for
-    split-BF16 factors with nb a multiple of 256 nb/2 wide from the first multiple of nb at
-    or after order n - tail_order (OOC_OPT_TAIL_ORDER)."""
+    """(J0, width) of the right-looking factor's panels, as the library schedules them: nb
+    wide, and for split-BF16 factors with nb a multiple of 256 nb/2 wide from the first
+    multiple of nb at or after order n - tail_order (OOC_OPT_TAIL_ORDER)."""
     t0 = n
     if prec == "bf16x3" and nb % 256 == 0 and n > nb and tail_order > 0:
         t0 = min(n, (max(0, n - tail_order) + nb - 1) // nb * nb)
@@ -723,6 +807,54 @@ def panel_schedule(n, nb, prec, tail_order):
         out.append((J0, min(nb // 2, n - J0)))
         J0 += nb // 2
     return out
+
+
+CATCH_K = 8192  # columns of K per long-K catch-up launch (kCatchK in csrc/mixed.cu)
+
+
+def lower_elems(m, cols):
+    """Lower-triangle elements of an m x m matrix in its first `cols` columns."""
+    cols = min(cols, m)
+    return cols * m - cols * (cols - 1) / 2
+
+
+def update_schedule(n, nb, prec, tail_order, block_cols, device_matrix=True):
+    """The factor's panels and trailing-update launches as (m, K, cols), mirroring the
+    library: left-looking column blocks (OOC_OPT_BLOCK_COLS; automatic: 4096 columns for a
+    stored matrix of order above 8192) with nb/2-wide panels, each block caught up by
+    long-K launches of at most CATCH_K columns of K and factored right-looking inside
+    itself and into the next block's first panel; otherwise right-looking over the whole
+    matrix, one update per panel (the narrow and bulk launches of a panel together)."""
+    bc = block_cols if block_cols >= 0 else (4096 if device_matrix and n > 8192 else 0)
+    lb = prec == "bf16x3" and nb % 128 == 0 and n > nb and bc > 0
+    if not lb:
+        panels = panel_schedule(n, nb, prec, tail_order)
+        return {"kind": "right-looking", "panels": panels,
+                "launches": [(n - J0 - LN, LN, n - J0 - LN) for J0, LN in panels if n - J0 - LN > 0]}
+    w = nb // 2 if nb % 256 == 0 else nb
+    panels = [(J0, min(w, n - J0)) for J0 in range(0, n, w)]
+    starts = [J0 for J0, _ in panels] + [n]
+    blocks, p = [], 0
+    while p < len(panels):
+        q = p + 1
+        while q < len(panels) and starts[q] - starts[p] < bc:
+            q += 1
+        blocks.append((p, q))
+        p = q
+    launches = []
+    for p0, p1 in blocks:
+        c0, cf, c1 = starts[p0], starts[p0 + 1], starts[p1]
+        cn = starts[min(p1, len(panels) - 1) + 1]
+        for c, wcols in ((c1, cn - c1), (cf, c1 - cf)):  # catch-ups of F_{b+1} and the rest
+            if c0 > 0 and wcols > 0:
+                for k0 in range(0, c0, CATCH_K):
+                    launches.append((n - c, min(CATCH_K, c0 - k0), wcols))
+        for j in range(p0, p1):
+            J0, LN = panels[j]
+            m = n - J0 - LN
+            if m > 0:
+                launches.append((m, LN, cn - J0 - LN))
+    return {"kind": f"left-looking blocks of {bc} columns", "panels": panels, "launches": launches}
 
 
 # ----------------------------------------------------------------------------------

@@ -69,12 +69,24 @@ enum {
                               n - value, are nb/2 wide (their one-CTA diagonal tiles are
                               ~3x cheaper where the trailing update no longer hides
                               them); 0 = uniform nb-wide panels.  Default 24576.      */
-  OOC_OPT_POOL_BYTES = 8   /* device bytes the handle may keep cached from destroyed
+  OOC_OPT_POOL_BYTES = 8,  /* device bytes the handle may keep cached from destroyed
                               factor objects for reuse by later ones of the same sizes
                               (freeing multi-GB buffers costs ~0.4 ms per GB and
                               synchronises the device); released by ooc_destroy, or when
                               an allocation fails.  Default 40 % of device memory, 0 =
                               no caching.                                             */
+  OOC_OPT_BLOCK_COLS = 9   /* split-BF16 factors of a stored matrix (nb a multiple of
+                              128): width, in columns (rounded up to whole panels), of the
+                              left-looking column blocks.  A block is caught up with every
+                              finished panel by long-K tensor-core updates, then factored
+                              right-looking inside itself in nb/2-wide panels; for a
+                              page-locked host matrix each block is copied to the device
+                              while earlier ones are factored (the reference's panel
+                              streaming, oocdag.cpp:59-87).  0 = right-looking over the
+                              whole matrix (a host matrix is copied first); -1 (default)
+                              = 4096 for device and page-locked host matrices with
+                              n > 8192, 0 otherwise.  Needs a plane store of 4 n^2
+                              device bytes while the factor is computed.              */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */

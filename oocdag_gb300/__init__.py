@@ -37,6 +37,7 @@ OPT_REF_SCHEDULE = 5
 OPT_KEEP_A = 6
 OPT_TAIL_ORDER = 7
 OPT_POOL_BYTES = 8
+OPT_BLOCK_COLS = 9
 
 PREC_FP64 = 0
 PREC_FP32 = 1

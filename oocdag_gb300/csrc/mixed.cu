@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1278,6 +1279,11 @@ size_t bf16x3_work_bytes(int m, int K);
 int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, size_t work_bytes, cudaStream_t s);
 int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
                            int K, void* swork, size_t sbytes, const int* status, cudaStream_t s);
+int launch_trsm_bf16x3_f32_to(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
+                              int K, void* ohi, void* olo, i64 ldo, const int* status, cudaStream_t s);
+int launch_syrk_planes_f32(const void* hi, const void* lo, i64 ldk, int m, int K, float* C, i64 ldc,
+                           const int* status, cudaStream_t s, unsigned long long* tickets, int bj_lo, int bj_hi,
+                           int reserve_sms);
 
 namespace {
 
@@ -1310,6 +1316,14 @@ struct DevBuf {
     if (!p) return OOC_ERR_NOMEM;
     bytes = b;
     return OOC_OK;
+  }
+  // gives the buffer back (to the pool, or freed) once the work queued on it is done
+  void release() {
+    if (!p) return;
+    if (pool) pool->release(p);
+    else cudaFree(p);
+    p = nullptr;
+    bytes = 0;
   }
 };
 
@@ -2047,6 +2061,281 @@ int factor_f32(ooc_factor* F, int prec, cudaStream_t s0, cudaStream_t s1, int64_
   return OOC_OK;
 }
 
+// Lower-triangle elements of an m x m trailing matrix in columns [a, b): the useful
+// outputs of an update restricted to those columns (2 K flops each).
+double lower_elems(i64 m, i64 a, i64 b) {
+  b = std::min(b, m);
+  if (a >= b) return 0.0;
+  return (double)(b - a) * (double)m - ((double)b * (double)(b - 1) - (double)a * (double)(a - 1)) / 2.0;
+}
+
+// Where the columns of a left-looking factorization come from: a page-locked host matrix
+// (copied on the copy stream, into the kept FP64 copy or through a ring of staging
+// slots) or a device matrix (converted in place).  Every column block reaches the FP32
+// working matrix through k_lower_conv on the compute stream.
+struct LbSource {
+  const double* A = nullptr;
+  i64 lda = 0;
+  bool on_device = false;
+  double* keep = nullptr;    // FP64 copy of the lower triangle (ld n), kept for the refinement
+  double* stage = nullptr;   // otherwise: `slots` staging slots of n x chunk doubles
+  int slots = 0;
+  i64 chunk = 512;           // columns per copy (at most 256 MB of full column height)
+};
+
+// Split-BF16 factorization of the FP32 working matrix F->Lf over left-looking column
+// blocks (the reference's panel streaming, oocdag.cpp:59-87: A2Y of a panel, its update by
+// every finished column, then the in-core factorization; here a block of whole panels).
+// Block b covers columns [c0, c1); F_b is its first panel, F_{b+1} the next block's.
+//   sc  copies the host matrix's lower triangle, chunk after chunk in column order, as
+//       far ahead as the staging allows (all of it when a kept copy is the destination);
+//   s0  converts each chunk to FP32 when it is needed.  At block b's start F_b is already
+//       up to date, so s1 factors its diagonal tile at once while s0 catches the rest of
+//       the block and F_{b+1} up with all panels before the block (long-K tensor-core
+//       updates from the plane store, at most kCatchK columns of K per launch).  The
+//       block's panels then go right-looking: column solve (writing its BF16 planes into
+//       the plane store: row r, column k of L at r * ldk + k), the next panel's columns
+//       first (an event lets s1 start on its diagonal tile), then the rest of the block
+//       and F_{b+1}, so that F_{b+1} is final when the block ends.  The in-block updates
+//       span at most a block's width, so the panels are narrow (nb/2 where nb is a
+//       multiple of 256): their diagonal tiles are factored in shared memory, quickly
+//       enough to hide behind those updates;
+//   s1  the one-CTA diagonal kernels, beside s0's bulk updates, as in factor_f32.
+// Long-K catch-ups move C once per kCatchK columns of K instead of once per panel, which
+// is what makes the tensor pipe busier than in the right-looking factor_f32.
+// Requires the tensor-core column solve (nb and nb2 multiples of 128).
+constexpr i64 kCatchK = 8192;
+
+int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t sc, i64 block_cols,
+                  const LbSource& src, int64_t* launches, MixedProf* prof) {
+  const i64 n = F->n;
+  const int nb = F->nb;
+  const Panels P = F->panels();
+  const int bb = P.count();
+  float* A = F->Lf;
+  const i64 lda = F->ld;
+  const i64 tile = (i64)nb * nb;
+  if (nb > DG_MAX || nb % 128 || P.nb2 % 128 || n <= nb || lda != n) return OOC_ERR_UNSUPPORTED;
+  if (!src.on_device && !src.keep && (!src.stage || src.slots < 1)) return OOC_ERR_INTERNAL;
+  int rc = F->scratch.ensure((size_t)tile * (sizeof(float) + 2 * sizeof(__nv_bfloat16)));
+  if (rc) return rc;
+  float* Xr = (float*)F->scratch.p;
+  __nv_bfloat16* Xh = reinterpret_cast<__nv_bfloat16*>(Xr + tile);
+  __nv_bfloat16* Xl = Xh + tile;
+  const size_t pb = bf16x3_work_bytes((int)(n - std::min(nb, P.nb2)), nb);
+  if ((rc = F->work2.ensure(pb))) return rc;
+  // plane store: hi then lo, n rows of ldk BF16 each, then the update launches' tickets
+  const i64 ldk = (n + 63) / 64 * 64;
+  const size_t plane = (size_t)n * (size_t)ldk;
+  if ((rc = F->work.ensure(2 * plane * sizeof(__nv_bfloat16) + 256))) return rc;
+  __nv_bfloat16* Ghi = (__nv_bfloat16*)F->work.p;
+  __nv_bfloat16* Glo = Ghi + plane;
+  unsigned long long* tickets = reinterpret_cast<unsigned long long*>(Glo + plane);
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_s256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DS_SMEM));
+  auto panel = [&](int p, i64* J0, int* LN) {
+    i64 off;
+    int ld;
+    P.get(p, J0, LN, &off, &ld);
+  };
+  auto col_of = [&](int q) -> i64 {  // first column of panel q (n past the last)
+    if (q >= bb) return n;
+    i64 J0;
+    int LN;
+    panel(q, &J0, &LN);
+    return J0;
+  };
+  // blocks of whole panels: [first panel, one past the last)
+  std::vector<std::pair<int, int>> blocks;
+  for (int p = 0; p < bb;) {
+    const i64 c0 = col_of(p);
+    int q = p + 1;
+    while (q < bb && (block_cols <= 0 || col_of(q) - c0 < block_cols)) q++;
+    blocks.emplace_back(p, q);
+    p = q;
+  }
+  const int nblocks = (int)blocks.size();
+  // chunks (the unit of copy and conversion): each panel's columns, split to at most
+  // src.chunk columns, in column order -- the order s0 converts them in
+  struct Chunk { i64 c0, c1; };
+  std::vector<Chunk> chunks;
+  std::vector<std::pair<int, int>> panel_chunks(bb);  // [first chunk, one past the last)
+  const i64 cw = src.on_device ? n : std::max<i64>(1, src.chunk);
+  for (int q = 0; q < bb; q++) {
+    const int k0 = (int)chunks.size();
+    const i64 a = col_of(q), e = col_of(q + 1);
+    for (i64 c = a; c < e; c += cw) chunks.push_back({c, std::min(e, c + cw)});
+    panel_chunks[q] = {k0, (int)chunks.size()};
+  }
+  const int nchunks = (int)chunks.size();
+  std::vector<cudaEvent_t> evs;  // every event this call creates (destroyed on return)
+  struct EvGuard {
+    std::vector<cudaEvent_t>* v;
+    ~EvGuard() { for (cudaEvent_t e : *v) cudaEventDestroy(e); }
+  } guard{&evs};
+  auto new_event = [&](cudaEvent_t* e) -> int {
+    OOC_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    evs.push_back(*e);
+    return OOC_OK;
+  };
+  cudaEvent_t evA, evP;
+  if ((rc = new_event(&evA)) || (rc = new_event(&evP))) return rc;
+  std::vector<cudaEvent_t> evCopied(nchunks, nullptr), evFree(src.slots > 0 ? src.slots : 1, nullptr);
+  if (!src.on_device) {
+    for (auto& e : evCopied) if ((rc = new_event(&e))) return rc;
+    for (auto& e : evFree) if ((rc = new_event(&e))) return rc;
+  }
+  const unsigned gx = (unsigned)((n + 255) / 256);
+  // copies are enqueued in chunk order; with staging slots, chunk k waits until the
+  // conversion of chunk k - slots has freed its slot (enqueued on s0 before it)
+  int next_copy = 0, next_conv = 0;
+  OOC_CUDA_TRY(cudaEventRecord(evP, s0));  // the factor's buffers were set up on s0
+  OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evP, 0));
+  auto enqueue_copies = [&]() -> int {
+    if (src.on_device) return OOC_OK;
+    while (next_copy < nchunks && (src.keep || next_copy < next_conv + src.slots)) {
+      const Chunk& c = chunks[next_copy];
+      double* dst;
+      if (src.keep) {
+        dst = src.keep + c.c0 * n;
+      } else {
+        const int slot = next_copy % src.slots;
+        if (next_copy >= src.slots) OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evFree[slot], 0));
+        dst = src.stage + (size_t)slot * (size_t)n * (size_t)src.chunk;
+      }
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(dst + c.c0, n * sizeof(double), src.A + c.c0 + c.c0 * src.lda,
+                                     src.lda * sizeof(double), (n - c.c0) * sizeof(double), c.c1 - c.c0,
+                                     cudaMemcpyHostToDevice, sc));
+      OOC_CUDA_TRY(cudaEventRecord(evCopied[next_copy], sc));
+      next_copy++;
+    }
+    return OOC_OK;
+  };
+  auto convert_panel = [&](int q) -> int {
+    for (int k = panel_chunks[q].first; k < panel_chunks[q].second; k++) {
+      const Chunk& c = chunks[k];
+      const int w = (int)(c.c1 - c.c0);
+      const double* from;
+      i64 ldf = n;
+      if (src.on_device) {
+        from = src.A + c.c0 * src.lda;
+        ldf = src.lda;
+      } else {
+        OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evCopied[k], 0));
+        from = src.keep ? src.keep + c.c0 * n : src.stage + (size_t)(k % src.slots) * (size_t)n * (size_t)src.chunk;
+      }
+      k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min(w, 1024)), 256, 0, s0>>>(from, ldf, A + c.c0 * lda,
+                                                                                       lda, n, c.c0, w, 0);
+      OOC_CUDA_TRY(cudaGetLastError());
+      if (!src.on_device && !src.keep) OOC_CUDA_TRY(cudaEventRecord(evFree[k % src.slots], s0));
+      next_conv = k + 1;
+      if (launches) *launches += 1;
+      if ((rc = enqueue_copies())) return rc;
+    }
+    return OOC_OK;
+  };
+  // C = trailing matrix from column `c` (rows c..n-1), columns [c, c + w), minus the
+  // contribution of the finished panels in columns [0, K): long-K updates from the store
+  auto catch_up = [&](i64 c, i64 w, i64 K) -> int {
+    if (K <= 0 || w <= 0) return OOC_OK;
+    const i64 m = n - c;
+    float* C = A + c * (1 + lda);
+    if (prof->on) {
+      prof->mark(s0);
+      prof->kind.push_back(1);
+      prof->flops.push_back(2.0 * (double)K * lower_elems(m, 0, w));
+    }
+    for (i64 k0 = 0; k0 < K; k0 += kCatchK) {
+      const i64 kw = std::min(kCatchK, K - k0);
+      int r = launch_syrk_planes_f32(Ghi + c * ldk + k0, Glo + c * ldk + k0, ldk, (int)m, (int)kw, C, lda, F->status,
+                                     s0, tickets, 0, (int)((w + 127) / 128), kChainSMs);
+      if (r) return r;
+      if (launches) *launches += 1;
+    }
+    if (prof->on) prof->mark(s0);
+    return OOC_OK;
+  };
+  auto split_raw = [&](i64 J0, int LN) -> int {  // panel's rows below its diagonal tile -> work2
+    const i64 m = n - J0 - LN;
+    if (m <= 0) return OOC_OK;
+    if (launches) *launches += 1;
+    return launch_split_bf16_f32(A + J0 + LN + J0 * lda, lda, (int)m, LN, F->work2.p, F->work2.bytes, s0);
+  };
+  if ((rc = enqueue_copies())) return rc;
+  if ((rc = convert_panel(0))) return rc;  // F_0
+  OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+  {
+    i64 J0;
+    int LN;
+    panel(0, &J0, &LN);
+    if ((rc = split_raw(J0, LN))) return rc;
+  }
+  for (int b = 0; b < nblocks; b++) {
+    const int p0 = blocks[b].first, p1 = blocks[b].second;
+    const i64 c0 = col_of(p0), cf = col_of(p0 + 1), c1 = col_of(p1);
+    const int plast = std::min(p1, bb - 1);  // the block's panels after F_b, and F_{b+1}
+    const i64 cn = col_of(plast + 1);         // end of the columns the block's updates reach
+    // F_b is final: s1 may factor its diagonal tile (after evA) while s0 converts the rest
+    // of the block and F_{b+1} and catches them up with every panel before the block.
+    for (int q = p0 + 1; q <= plast; q++)
+      if ((rc = convert_panel(q))) return rc;
+    if ((rc = catch_up(c1, cn - c1, c0))) return rc;  // F_{b+1}
+    if ((rc = catch_up(cf, c1 - cf, c0))) return rc;  // the rest of block b
+    for (int j = p0; j < p1; j++) {
+      i64 J0, off;
+      int LN, ldd;
+      P.get(j, &J0, &LN, &off, &ldd);
+      float* Djj = A + J0 + J0 * lda;
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
+      if (prof->on) { prof->mark(s1); prof->kind.push_back(0); }
+      if (LN <= DS_MAX)
+        k_diag_s256<<<1, DG_THREADS, DS_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
+      else
+        k_diag_f32<<<1, DG_THREADS, DG_SMEM, s1>>>(Djj, lda, LN, J0, F->Dinvf + off, ldd, Xr, Xh, Xl, F->status);
+      OOC_CUDA_TRY(cudaGetLastError());
+      if (prof->on) prof->mark(s1);
+      OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+      if (launches) *launches += 1;
+      const i64 m = n - J0 - LN;
+      if (m <= 0) continue;
+      float* Pn = Djj + LN;
+      __nv_bfloat16* gh = Ghi + (J0 + LN) * ldk + J0;  // this panel's rows below its diagonal tile
+      __nv_bfloat16* gl = Glo + (J0 + LN) * ldk + J0;
+      if (prof->on) { prof->mark(s0); prof->kind.push_back(0); }
+      rc = launch_trsm_bf16x3_f32_to(F->work2.p, F->work2.bytes, Xh, Xl, Pn, lda, (int)m, LN, gh, gl, ldk, F->status,
+                                     s0);
+      if (rc) return rc;
+      if (prof->on) prof->mark(s0);
+      if (launches) *launches += 1;
+      // right-looking inside the block, and into F_{b+1}: columns [J0 + LN, cn)
+      i64 J0n;
+      int LNn;
+      panel(j + 1, &J0n, &LNn);
+      const i64 wa = cn - J0 - LN;
+      const int bjn = (LNn + 127) / 128;
+      const int bjh = (int)((wa + 127) / 128);
+      float* C = A + (J0 + LN) * (1 + lda);
+      if (prof->on) {
+        prof->mark(s0);
+        prof->kind.push_back(1);
+        prof->flops.push_back(2.0 * (double)LN * lower_elems(m, 0, wa));
+      }
+      rc = launch_syrk_planes_f32(gh, gl, ldk, (int)m, LN, C, lda, F->status, s0, tickets, 0, bjn, 0);
+      if (rc) return rc;
+      OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+      if ((rc = split_raw(J0n, LNn))) return rc;
+      rc = launch_syrk_planes_f32(gh, gl, ldk, (int)m, LN, C, lda, F->status, s0, tickets, bjn, bjh, kChainSMs);
+      if (rc) return rc;
+      if (prof->on) prof->mark(s0);
+      if (launches) *launches += 2;
+    }
+  }
+  OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+  OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
+  return OOC_OK;
+}
+
 int read_int(const int* d, int* h, cudaStream_t s) {
   OOC_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
   OOC_CUDA_TRY(cudaStreamSynchronize(s));
@@ -2079,7 +2368,30 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   F->prec = prec;
   F->tail0 = n;
   F->nb2 = nb;
-  if (prec == OOC_PREC_BF16X3 && nb % 256 == 0 && n > nb) {  // nb/2-wide tail panels
+  // Left-looking column blocks (OOC_OPT_BLOCK_COLS) for split-BF16 factors of a stored
+  // matrix: the blocks are filled on the third stream while earlier ones are factored.
+  bool on_device = false, pinned = false;
+  if (!gen) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, A) == cudaSuccess) {
+      on_device = pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged;
+      pinned = pa.type == cudaMemoryTypeHost;
+    }
+    cudaGetLastError();
+  }
+  i64 bcols = 0;
+  {
+    int64_t opt = -1;
+    ooc_get_option(h, OOC_OPT_BLOCK_COLS, &opt);
+    // automatic: 4096-column blocks for device and page-locked host matrices of more
+    // than two blocks (faster long-K updates; for a host matrix, copies overlapped)
+    bcols = opt >= 0 ? opt : ((pinned || on_device) && n > 2 * 4096 ? 4096 : 0);
+  }
+  const bool lb = !gen && bcols > 0 && prec == OOC_PREC_BF16X3 && nb % 128 == 0 && n > nb && (on_device || pinned);
+  if (lb && nb % 256 == 0) {  // left-looking blocks: nb/2-wide panels throughout
+    F->tail0 = 0;
+    F->nb2 = nb / 2;
+  } else if (prec == OOC_PREC_BF16X3 && nb % 256 == 0 && n > nb) {  // nb/2-wide tail panels
     int64_t tail = 0;
     ooc_get_option(h, OOC_OPT_TAIL_ORDER, &tail);
     if (tail > 0) {
@@ -2098,6 +2410,43 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
   // A (generated, host or device) into the factor's storage
   rc = OOC_OK;
   if (cudaMemsetAsync(F->status, 0, sizeof(int), s) != cudaSuccess) rc = OOC_ERR_CUDA;
+  int64_t keep = 0;
+  if (!gen && !on_device) ooc_get_option(h, OOC_OPT_KEEP_A, &keep);
+  if (!rc && keep && reduced) {
+    if (F->alloc(&F->A64, (size_t)n * n * sizeof(double))) {
+      rc = OOC_ERR_NOMEM;
+    } else {
+      F->A64_src = A;
+      F->A64_lda = lda;
+    }
+  }
+  DevBuf stage;  // host columns on their way to the FP32 matrix when no copy is kept
+  const unsigned gx = (unsigned)((n + 255) / 256);
+  // columns [c0, c1) of A (rows c0..n-1) into the FP32 working matrix, on stream `st`
+  std::function<int(i64, i64, cudaStream_t)> fill = [&](i64 c0, i64 c1, cudaStream_t st) -> int {
+    if (on_device) {
+      k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(c1 - c0, 1024)), 256, 0, st>>>(
+          A + c0 * lda, lda, F->Lf + c0 * n, n, n, c0, (int)(c1 - c0), 0);
+      return cudaGetLastError() == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+    }
+    // chunks of at most 256 MB of a full column height: the copy follows the lower
+    // triangle chunk by chunk (rows k0..n-1 of columns k0..k0+wc-1)
+    const i64 w = std::max<i64>(1, std::min<i64>(c1 - c0, (256LL << 20) / (8 * n)));
+    if (!keep) {
+      int r = stage.ensure((size_t)n * w * sizeof(double));
+      if (r) return r;
+    }
+    for (i64 k0 = c0; k0 < c1; k0 += w) {  // the lower part of each column block (rows k0..n-1)
+      const int wc = (int)std::min<i64>(w, c1 - k0);
+      double* dst = keep ? F->A64 + k0 * n : (double*)stage.p;  // column k0 of the block, ld n
+      if (cudaMemcpy2DAsync(dst + k0, n * sizeof(double), A + k0 + k0 * lda, lda * sizeof(double),
+                            (n - k0) * sizeof(double), wc, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return OOC_ERR_CUDA;
+      k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min(wc, 1024)), 256, 0, st>>>(dst, n, F->Lf + k0 * n, n,
+                                                                                        n, k0, wc, 0);
+    }
+    return cudaGetLastError() == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
+  };
   if (!rc && !reduced) {
     if (gen) {
       rc = launch_gen_uniform_block(F->L, n, n, seed, alpha, 0, 0, n, n, s);
@@ -2105,47 +2454,13 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
                                  cudaMemcpyDefault, s) != cudaSuccess) {
       rc = OOC_ERR_CUDA;
     }
-  } else if (!rc) {
-    const unsigned gx = (unsigned)((n + 255) / 256);
+  } else if (!rc && !lb) {
     if (gen) {
       k_gen_uniform_f32_lower<<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256, 0, s>>>(
           F->Lf, n, n, ooc_uniform_key(seed), alpha);
     } else {
-      cudaPointerAttributes pa{};
-      const bool on_device = cudaPointerGetAttributes(&pa, A) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
-      cudaGetLastError();
-      if (on_device) {
-        k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(n, 1024)), 256, 0, s>>>(A, lda, F->Lf, n, n,
-                                                                                             0, (int)n, 0);
-      } else {  // host matrix: the lower part of each column block (rows c0..n-1), either
-                // into the kept FP64 copy (OOC_OPT_KEEP_A) or through a staging buffer
-        int64_t keep = 0;
-        ooc_get_option(h, OOC_OPT_KEEP_A, &keep);
-        const int w = (int)std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
-        DevBuf stage;
-        if (keep) {
-          if (F->alloc(&F->A64, (size_t)n * n * sizeof(double))) {
-            rc = OOC_ERR_NOMEM;
-          } else {
-            F->A64_src = A;
-            F->A64_lda = lda;
-          }
-        } else {
-          rc = stage.ensure((size_t)n * w * sizeof(double));
-        }
-        for (i64 c0 = 0; !rc && c0 < n; c0 += w) {
-          const int wc = (int)std::min<i64>(w, n - c0);
-          double* dst = keep ? F->A64 + c0 * n : (double*)stage.p;  // column c0 of the block, ld n
-          if (cudaMemcpy2DAsync(dst + c0, n * sizeof(double), A + c0 + c0 * lda, lda * sizeof(double),
-                                (n - c0) * sizeof(double), wc, cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            rc = OOC_ERR_CUDA;
-            break;
-          }
-          k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min(wc, 1024)), 256, 0, s>>>(
-              dst, n, F->Lf + c0 * n, n, n, c0, wc, 0);
-        }
-        if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = OOC_ERR_CUDA;  // before the staging buffer goes
-      }
+      rc = fill(0, n, s);
+      if (!rc && !on_device && cudaStreamSynchronize(s) != cudaSuccess) rc = OOC_ERR_CUDA;  // before `stage` goes
     }
     if (!rc && cudaGetLastError() != cudaSuccess) rc = OOC_ERR_CUDA;
   }
@@ -2160,12 +2475,30 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     cudaEventRecord(e0, s);
     void* s1p = nullptr;
     ooc_get_stream(h, 1, &s1p);
-    rc = reduced ? factor_f32(F, prec, s, (cudaStream_t)s1p, &launches, &prof)
-                 : factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);
+    if (lb) {
+      void* s2p = nullptr;
+      ooc_get_stream(h, 2, &s2p);
+      LbSource src;
+      src.A = A;
+      src.lda = lda;
+      src.on_device = on_device;
+      src.keep = keep ? F->A64 : nullptr;
+      src.chunk = std::max<i64>(1, std::min<i64>(n, (256LL << 20) / (8 * n)));
+      if (!on_device && !keep) {  // a ring of staging slots for the copies
+        src.slots = 8;
+        rc = stage.ensure((size_t)src.slots * (size_t)n * (size_t)src.chunk * sizeof(double));
+        src.stage = (double*)stage.p;
+      }
+      if (!rc) rc = factor_f32_lb(F, s, (cudaStream_t)s1p, (cudaStream_t)s2p, bcols, src, &launches, &prof);
+    } else {
+      rc = reduced ? factor_f32(F, prec, s, (cudaStream_t)s1p, &launches, &prof)
+                   : factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);
+    }
     cudaEventRecord(e1, s);
   }
   int st = 0;
   if (!rc) rc = read_int(F->status, &st, s);
+  if (lb) F->work.release();  // the plane store: the factor is complete
   if (!rc) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { ooc_set_last_error(e, "mixed factorization", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }

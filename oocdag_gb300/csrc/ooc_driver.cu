@@ -70,6 +70,7 @@ struct ooc_handle {
   int ref_schedule = 0;
   int keep_a = 0;
   int64_t tail_order = 24576;
+  int64_t block_cols = -1;  // OOC_OPT_BLOCK_COLS (-1: by input)
   std::shared_ptr<DevPool> pool;  // device buffers of the handle's factor objects
   int last_info = 0;
   std::vector<cudaEvent_t> ev_pool;  // reusable timing-free events
@@ -219,6 +220,10 @@ extern "C" int ooc_set_option(ooc_handle* h, int key, int64_t v) {
       if (v < 0) return -3;
       if (h->pool) h->pool->set_cap((size_t)v);
       return OOC_OK;
+    case OOC_OPT_BLOCK_COLS:
+      if (v < -1) return -3;
+      h->block_cols = v;
+      return OOC_OK;
     default: return -2;
   }
 }
@@ -235,6 +240,7 @@ extern "C" int ooc_get_option(ooc_handle* h, int key, int64_t* v) {
     case OOC_OPT_KEEP_A: *v = h->keep_a; return OOC_OK;
     case OOC_OPT_TAIL_ORDER: *v = h->tail_order; return OOC_OK;
     case OOC_OPT_POOL_BYTES: *v = h->pool ? (int64_t)h->pool->cap : 0; return OOC_OK;
+    case OOC_OPT_BLOCK_COLS: *v = h->block_cols; return OOC_OK;
     default: return -2;
   }
 }

@@ -790,7 +790,7 @@ __global__ void __launch_bounds__(THREADS2, 1)
     k_trsm2_bf16x3(const __grid_constant__ CUtensorMap map_uhi, const __grid_constant__ CUtensorMap map_ulo,
                    const __grid_constant__ CUtensorMap map_xhi, const __grid_constant__ CUtensorMap map_xlo,
                    float* __restrict__ P, i64 ldp, __nv_bfloat16* __restrict__ shi, __nv_bfloat16* __restrict__ slo,
-                   int Kp, int m, int ncb, i64 nblk, unsigned long long* __restrict__ tickets, int* status) {
+                   i64 lds, int Kp, int m, int ncb, i64 nblk, unsigned long long* __restrict__ tickets, int* status) {
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -962,8 +962,8 @@ __global__ void __launch_bounds__(THREADS2, 1)
         if ((2 * bi2 + h) * TB >= m) continue;  // uniform: this half was not computed
         const int row = (2 * bi2 + h) * TB + quad * 32 + lane, c0 = cb * TB + cg;
         float* pb = P + row + (i64)c0 * ldp;
-        __nv_bfloat16* hb = shi + (i64)row * Kp + c0;
-        __nv_bfloat16* lb = slo + (i64)row * Kp + c0;
+        __nv_bfloat16* hb = shi + (i64)row * lds + c0;
+        __nv_bfloat16* lb = slo + (i64)row * lds + c0;
         const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + h * TB + cg);
 #pragma unroll
         for (int ch = 0; ch < 4; ch++) {
@@ -1041,9 +1041,11 @@ int get_encode() {
   return g_encode ? OOC_OK : OOC_ERR_UNSUPPORTED;
 }
 
-int make_map(CUtensorMap* map, void* base, int Mp, int Kp, int box_rows = TB) {
-  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)Mp};
-  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+// BF16 plane of `rows` rows of K values (row-major, `ldk` elements between rows; ldk = K
+// when omitted): boxes of TK x box_rows.  Rows and K past the plane read as zeros.
+int make_map(CUtensorMap* map, void* base, int rows, int K, int box_rows = TB, i64 ldk = 0) {
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ldk > 0 ? ldk : K) * 2};
   cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
@@ -1185,14 +1187,15 @@ int launch_split_bf16_f32(const float* X, i64 ldx, int m, int K, void* work, siz
 // Column solve of an FP32 panel on the tensor cores, P = U X^T (k_trsm2_bf16x3).  `uwork`
 // holds the planes of the panel before the solve (launch_split_bf16_f32, m x K) followed by
 // the 256 bytes of block tickets; `xhi`, `xlo` the hi and lo planes of X = L_jj^{-1}
-// (K x K, row-major, ld K).  The result goes to P (ld ldp) and, split, to the planes at `swork` in the
-// layout launch_syrk_bf16x3_f32 reads with do_split = 0.  K must be a multiple of 128.
-int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
-                           int K, void* swork, size_t sbytes, const int* status, cudaStream_t s) {
+// (K x K, row-major, ld K).  The result goes to P (ld ldp) and, split, to the planes `ohi`,
+// `olo` (row r's K values at r * ldo; rows past m are not written).  K must be a multiple
+// of 128.
+int launch_trsm_bf16x3_f32_to(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
+                              int K, void* ohi, void* olo, i64 ldo, const int* status, cudaStream_t s) {
   if (m <= 0 || K <= 0) return OOC_OK;
   if (K % TB != 0) return OOC_ERR_UNSUPPORTED;
-  if (!status || !uwork || !xhi || !xlo || !swork) return OOC_ERR_INTERNAL;
-  if (ubytes < bf16x3_work_bytes(m, K) || sbytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
+  if (!status || !uwork || !xhi || !xlo || !ohi || !olo || ldo < K) return OOC_ERR_INTERNAL;
+  if (ubytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
   int rc = get_encode();
   if (rc) return rc;
   const int Mp = (m + TB - 1) / TB * TB, Kp = K;
@@ -1201,8 +1204,6 @@ int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const vo
   unsigned long long* tickets = reinterpret_cast<unsigned long long*>(ul + (size_t)Mp * Kp);
   __nv_bfloat16* xh = (__nv_bfloat16*)const_cast<void*>(xhi);
   __nv_bfloat16* xl = (__nv_bfloat16*)const_cast<void*>(xlo);
-  __nv_bfloat16* sh = (__nv_bfloat16*)swork;
-  __nv_bfloat16* sl = sh + (size_t)Mp * Kp;
   CUtensorMap mu_h, mu_l, mx_h, mx_l;
   if (make_map(&mu_h, uh, Mp, Kp, TM2) || make_map(&mu_l, ul, Mp, Kp, TM2) || make_map(&mx_h, xh, K, K, TB) ||
       make_map(&mx_l, xl, K, K, TB)) {
@@ -1217,8 +1218,74 @@ int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const vo
   const i64 grid = std::max<i64>(1, std::min<i64>(nblk, nsm));
   OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm2_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2_BYTES));
   OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
-  k_trsm2_bf16x3<<<(unsigned)grid, THREADS2, SMEM2_BYTES, s>>>(mu_h, mu_l, mx_h, mx_l, P, ldp, sh, sl, Kp, m, ncb,
-                                                              nblk, tickets, const_cast<int*>(status));
+  k_trsm2_bf16x3<<<(unsigned)grid, THREADS2, SMEM2_BYTES, s>>>(mu_h, mu_l, mx_h, mx_l, P, ldp, (__nv_bfloat16*)ohi,
+                                                              (__nv_bfloat16*)olo, ldo, Kp, m, ncb, nblk, tickets,
+                                                              const_cast<int*>(status));
+  OOC_CUDA_TRY(cudaGetLastError());
+  return OOC_OK;
+}
+
+// The same with the result planes in `swork`, in the layout launch_syrk_bf16x3_f32 reads
+// with do_split = 0 (Mp x K, hi then lo).
+int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const void* xlo, float* P, i64 ldp, int m,
+                           int K, void* swork, size_t sbytes, const int* status, cudaStream_t s) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (!swork || sbytes < bf16x3_work_bytes(m, K)) return OOC_ERR_INTERNAL;
+  const size_t Mp = ((size_t)m + TB - 1) / TB * TB;
+  __nv_bfloat16* sh = (__nv_bfloat16*)swork;
+  return launch_trsm_bf16x3_f32_to(uwork, ubytes, xhi, xlo, P, ldp, m, K, sh, sh + Mp * (size_t)K, K, status, s);
+}
+
+// FP32 trailing matrix C (m x m, lower, ld ldc) -= X X^T restricted to the 128-wide block
+// columns [bj_lo, bj_hi) (bj_hi < 0 = all), with X given as BF16 hi/lo planes already split:
+// row r's K values at hi + r * ldk, lo + r * ldk (for example a window of a matrix-wide
+// plane store: rows from the trailing matrix's first row, K over any run of finished
+// panels).  `tickets` is 8 bytes of device memory for the launch's block counter.
+int launch_syrk_planes_f32(const void* hi, const void* lo, i64 ldk, int m, int K, float* C, i64 ldc,
+                           const int* status, cudaStream_t s, unsigned long long* tickets, int bj_lo, int bj_hi,
+                           int reserve_sms) {
+  if (m <= 0 || K <= 0) return OOC_OK;
+  if (!status || !hi || !lo || !tickets || K % TK != 0 || ldk < K) return OOC_ERR_INTERNAL;
+  if ((reinterpret_cast<uintptr_t>(hi) | reinterpret_cast<uintptr_t>(lo) | (uintptr_t)(ldk * 2)) % 16 != 0)
+    return OOC_ERR_INTERNAL;
+  int rc = get_encode();
+  if (rc) return rc;
+  void* h = const_cast<void*>(hi);
+  void* l = const_cast<void*>(lo);
+  const i64 T = ((i64)m + TB - 1) / TB;
+  bj_hi = (int)std::min<i64>(bj_hi < 0 ? T : bj_hi, T);
+  if (bj_lo >= bj_hi) return OOC_OK;
+  int dev = 0, nsm = 0;
+  OOC_CUDA_TRY(cudaGetDevice(&dev));
+  OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CUtensorMap mh, ml;
+  if (make_map(&mh, h, m, K, TB, ldk) || make_map(&ml, l, m, K, TB, ldk)) {
+    ooc_set_last_message("cuTensorMapEncodeTiled failed for the plane-store window");
+    return OOC_ERR_CUDA;
+  }
+  if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && (ldc * (i64)sizeof(float)) % 16 == 0) {
+    CUtensorMap ah, al, mc;
+    if (make_map(&ah, h, m, K, TM2, ldk) || make_map(&al, l, m, K, TM2, ldk) || make_map_c32(&mc, C, m, ldc)) {
+      ooc_set_last_message("cuTensorMapEncodeTiled failed for the update operands");
+      return OOC_ERR_CUDA;
+    }
+    const i64 nblk2 = count_blocks2((int)T, bj_lo, bj_hi);
+    if (nblk2 <= 0) return OOC_OK;
+    OOC_CUDA_TRY(
+        cudaFuncSetAttribute(k_syrk2_bf16x3<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2U_BYTES));
+    const i64 grid2 = std::max<i64>(1, std::min<i64>(nblk2, std::max(1, nsm - std::max(0, reserve_sms))));
+    OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
+    k_syrk2_bf16x3<float><<<(unsigned)grid2, THREADS2, SMEM2U_BYTES, s>>>(ah, al, mh, ml, mc, m, K, (int)T, bj_lo,
+                                                                          bj_hi, nblk2, tickets,
+                                                                          const_cast<int*>(status));
+    OOC_CUDA_TRY(cudaGetLastError());
+    return OOC_OK;
+  }
+  const i64 nblk = ooc_lower_blocks_before(bj_hi, T) - ooc_lower_blocks_before(bj_lo, T);
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk_bf16x3<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+  const i64 grid = std::max<i64>(1, std::min<i64>(nblk, std::max(1, nsm - std::max(0, reserve_sms))));
+  k_syrk_bf16x3<float><<<(unsigned)grid, THREADS, SMEM_BYTES, s>>>(mh, ml, C, ldc, m, K, (int)T, bj_lo, bj_hi, nblk,
+                                                                  const_cast<int*>(status));
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }

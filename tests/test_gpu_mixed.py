@@ -316,3 +316,64 @@ def test_split_bf16_at_bench_tile_width_n16384(oracle_mod, handle, ooc, tail):
     assert _berr(A, X, B) <= 2 * BERR_TOL
     fwd = np.abs(X - Xo).max() / np.abs(Xo).max()
     assert fwd < FWD_TOL, fwd
+
+
+@pytest.mark.parametrize("where,keep,nb,bcols,n", [
+    ("host", 1, 512, -1, 10000),   # default: page-locked host matrix in 4096-column blocks
+    ("host", 0, 256, 1024, 5000),  # ragged last panel, staging instead of a kept copy
+    ("device", 0, 512, 2048, 9000),
+    ("device", 0, 256, 256, 2100),  # one panel per block
+])
+def test_left_looking_blocks(oracle_mod, handle, ooc, where, keep, nb, bcols, n):
+    # Split-BF16 factors over left-looking column blocks (OOC_OPT_BLOCK_COLS): each block is
+    # filled (copied from a page-locked host matrix while earlier blocks are factored, or
+    # converted from the device matrix), caught up with every finished panel by one long-K
+    # update from the plane store, then factored inside itself.  Against the oracle's FP64
+    # factor at the split-BF16 level, close to the right-looking factor of the same matrix,
+    # and refinement to the FP64 backward-error bar.
+    import torch
+
+    r = 2
+    A, _ = _c2_matrix(oracle_mod, n, 0.1)
+    B = np.asfortranarray(np.random.default_rng(8).standard_normal((n, r)))
+    Bd, Xd = _dev(B), _dev(np.zeros((n, r)))
+    Ain = torch.from_numpy(np.ascontiguousarray(A.T)).pin_memory() if where == "host" else _dev(A)
+    Lb = np.asfortranarray(np.full((n, n), np.nan))
+    Lr = np.asfortranarray(np.full((n, n), np.nan))
+    handle.set_option(ooc.OPT_KEEP_A, keep)
+    try:
+        handle.set_option(ooc.OPT_BLOCK_COLS, bcols)
+        with handle.factor(Ain, n, n, nb, "bf16x3") as F:
+            assert F.info == 0
+            F.copy_L(Lb, n)
+            it, be = F.refine(Ain, n, Bd, n, Xd, n, r, BERR_TOL, 30)
+        handle.set_option(ooc.OPT_BLOCK_COLS, 0)
+        with handle.factor(Ain, n, n, nb, "bf16x3") as F:
+            F.copy_L(Lr, n)
+    finally:
+        handle.set_option(ooc.OPT_BLOCK_COLS, -1)
+        handle.set_option(ooc.OPT_KEEP_A, 0)
+    Lo = A.copy(order="F")
+    oracle_mod.cholesky(Lo, nb, 1 << 40, 4, 2)
+    Lo = np.tril(Lo)
+    scale = np.abs(Lo).max()
+    assert np.abs(np.tril(Lb) - Lo).max() <= 1e-3 * scale
+    assert np.abs(np.tril(Lb) - np.tril(Lr)).max() <= 1e-4 * scale
+    assert np.all(np.triu(Lb, 1) == 0)
+    assert be <= BERR_TOL and it <= 5, (it, be)
+    assert _berr(A, _host(Xd), B) <= 2 * BERR_TOL
+
+
+def test_left_looking_blocks_report_lapack_info(oracle_mod, handle, ooc):
+    import torch
+
+    n, nb = 3000, 256
+    A = oracle_mod.gen_uniform(n, 1, float(n))
+    A[2222, 2222] = -5.0
+    Ah = torch.from_numpy(np.ascontiguousarray(A.T)).pin_memory()
+    handle.set_option(ooc.OPT_BLOCK_COLS, 512)
+    try:
+        with handle.factor(Ah, n, n, nb, "bf16x3") as F:
+            assert F.info == 2223
+    finally:
+        handle.set_option(ooc.OPT_BLOCK_COLS, -1)
