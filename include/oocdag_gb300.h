@@ -47,6 +47,9 @@ typedef struct ooc_stats {
   int64_t update_launches;
   double update_flops;     /* algorithmic flops of those launches                    */
   double factor_ms;        /* diagonal factor + column solve                         */
+  double h2d_ms;           /* host-to-device copies of a streamed host matrix: first
+                              copy's start to last copy's end on the copy stream
+                              (OOC_OPT_PROFILE; 0 otherwise)                        */
 } ooc_stats;
 
 /* Options (ooc_set_option). */

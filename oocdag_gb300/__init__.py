@@ -65,6 +65,7 @@ class OocStats(ctypes.Structure):
         ("update_launches", ctypes.c_int64),
         ("update_flops", ctypes.c_double),
         ("factor_ms", ctypes.c_double),
+        ("h2d_ms", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:

@@ -322,7 +322,8 @@ size_t smem_for(int blk) { return (size_t)(64 * 65 + NMAX * (blk + 1)) * sizeof(
 
 template <typename T>
 int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
-              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg);
+              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg,
+              GrowBuf* ws);
 
 template <typename T>
 int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off, T* A, T* B,
@@ -330,7 +331,8 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
   std::vector<Item> items(count);
   for (int i = 0; i < count; i++) items[i] = Item{(void*)(A + a_off[i]), (void*)(B + b_off[i]), n[i], 0, 0};
   return run_items<T>(ooc_compute_stream(h), ooc_device(h), items, info_host, blk_table, ctas_per_sm, do_solve, seconds,
-                      [](void* hh, cudaStream_t st) { return ooc_wait_stream((ooc_handle*)hh, st); }, (void*)h);
+                      [](void* hh, cudaStream_t st) { return ooc_wait_stream((ooc_handle*)hh, st); }, (void*)h,
+                      ooc_handle_batch_ws(h));
 }
 
 // Sorts the items by decreasing order, picks each one's panel width from the table, and
@@ -338,7 +340,8 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
 // the caller's order.
 template <typename T>
 int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
-              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg) {
+              int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg,
+              GrowBuf* ws) {
   const int count = (int)items_in.size();
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
@@ -355,14 +358,20 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
     items[i].blk = blk;
     maxblk = std::max(maxblk, blk);
   }
+  // the launch tables, in the caller's workspace (kept across calls): items, then four
+  // int arrays (info, order, scattered info, counter), each 256-byte aligned
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t b_items = up(sizeof(Item) * (size_t)count), b_int = up(sizeof(int) * (size_t)count);
+  int rc = ws->ensure(b_items + 3 * b_int + 256);
   Item* d_items = nullptr;
   int *d_info = nullptr, *d_order = nullptr, *d_out = nullptr, *d_counter = nullptr;
-  int rc = OOC_OK;
-  if (cudaMalloc(&d_items, sizeof(Item) * count) != cudaSuccess || cudaMalloc(&d_info, sizeof(int) * count) != cudaSuccess ||
-      cudaMalloc(&d_order, sizeof(int) * count) != cudaSuccess || cudaMalloc(&d_out, sizeof(int) * count) != cudaSuccess ||
-      cudaMalloc(&d_counter, sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();
-    rc = OOC_ERR_NOMEM;
+  if (!rc) {
+    char* base = (char*)ws->p;
+    d_items = (Item*)base;
+    d_info = (int*)(base + b_items);
+    d_order = (int*)(base + b_items + b_int);
+    d_out = (int*)(base + b_items + 2 * b_int);
+    d_counter = (int*)(base + b_items + 3 * b_int);
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (!rc) {
@@ -401,11 +410,6 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  cudaFree(d_items);
-  cudaFree(d_info);
-  cudaFree(d_order);
-  cudaFree(d_out);
-  cudaFree(d_counter);
   return rc;
 }
 
@@ -424,8 +428,9 @@ int check_args(int count, const int* n, const int64_t* a_off, const int64_t* b_o
 }  // namespace
 
 // Server hook: FP64 items given by absolute device pointers (mode 0 factor+solve, 1 solve).
+// `ws`: the caller's workspace for the launch tables (kept across calls).
 int ooc_batched_run_ptrs(cudaStream_t s, int dev, int count, double* const* a, double* const* b, const int* n,
-                         const int* mode, int* info_host, const int* blk_table) {
+                         const int* mode, int* info_host, const int* blk_table, GrowBuf* ws) {
   std::vector<Item> items(count);
   for (int i = 0; i < count; i++) items[i] = Item{(void*)a[i], (void*)b[i], n[i], 0, mode[i]};
   return run_items<double>(s, dev, items, info_host, blk_table, 0, 1, nullptr,
@@ -433,7 +438,7 @@ int ooc_batched_run_ptrs(cudaStream_t s, int dev, int count, double* const* a, d
                              cudaError_t e = cudaStreamSynchronize(st);
                              return e == cudaSuccess ? OOC_OK : OOC_ERR_CUDA;
                            },
-                           nullptr);
+                           nullptr, ws);
 }
 
 extern "C" int ooc_batched_dposv(ooc_handle* h, int count, const int* n, const int64_t* a_off, const int64_t* b_off,

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <memory>
 #include <stdint.h>
 #include <stdio.h>
@@ -94,6 +95,35 @@ ooc_handle* ooc_default_handle();
 // The handle's device-buffer cache (devpool.cuh), shared with the factor objects it creates.
 struct DevPool;
 std::shared_ptr<DevPool> ooc_handle_pool(ooc_handle* h);
+
+// Device scratch that only grows: kept across calls and reallocated only when a call needs
+// more than it holds (by at least half again, so that a slowly growing need reallocates a
+// few times only).  Reallocation frees the old buffer first; callers make sure no work that
+// uses it is still queued (every entry point waits for its streams before it returns).
+struct GrowBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t b) {
+    if (b <= bytes) return OOC_OK;
+    const size_t want = std::max(b, bytes + bytes / 2);
+    release();
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return OOC_ERR_NOMEM;
+    }
+    bytes = want;
+    return OOC_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  ~GrowBuf() { release(); }
+};
+// The handle's workspace for the batched solvers' launch tables.
+GrowBuf* ooc_handle_batch_ws(ooc_handle* h);
 
 // Generators (matgen.cu): fill the block of global rows [r0, r0+m) and columns
 // [c0, c0+nc) of the n x n test matrix into the device buffer B (leading dimension ldb).

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1789,6 +1790,10 @@ struct ooc_factor {
   std::shared_ptr<DevPool> pool;
   DevBuf part, partf, work, scratch;
   DevBuf work2;  // BF16 planes of the panel before its tensor-core column solve
+  // Solves share the buffers above: calls on one factor from several threads take turns.
+  std::mutex solve_mu;
+  DevBuf rws;    // refinement workspace (residual, FP32 correction, reductions), kept
+  DevBuf sws;    // FP32 right-hand sides of ooc_factor_solve on a reduced factor, kept
   DevBuf part2;  // partial sums of the refinement's norm (second stream)
   // FP64 copy of a host A's lower triangle (ld n), kept for the refinement
   // (OOC_OPT_KEEP_A); A64_src / A64_lda identify the host matrix it came from.
@@ -1844,13 +1849,19 @@ struct MixedProf {
   std::vector<cudaEvent_t> ev;  // pairs: [2k] start, [2k+1] end (on the segment's stream)
   std::vector<int> kind;        // 0 = FP64 factor + column solve, 1 = trailing update
   std::vector<double> flops;    // algorithmic flops of each update
+  cudaEvent_t h2d0 = nullptr, h2d1 = nullptr;  // first copy's start, last copy's end
+  double h2d_bytes = 0;         // bytes of a streamed host matrix copied to the device
   void mark(cudaStream_t s) {
     cudaEvent_t e;
     cudaEventCreate(&e);
     cudaEventRecord(e, s);
     ev.push_back(e);
   }
-  ~MixedProf() { for (cudaEvent_t e : ev) cudaEventDestroy(e); }
+  ~MixedProf() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (h2d0) cudaEventDestroy(h2d0);
+    if (h2d1) cudaEventDestroy(h2d1);
+  }
 };
 
 // Right-looking in-core FP64 factorization of F->L (ld n) (the reference's ooc_incore over
@@ -2203,10 +2214,19 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
         if (next_copy >= src.slots) OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evFree[slot], 0));
         dst = src.stage + (size_t)slot * (size_t)n * (size_t)src.chunk;
       }
+      if (prof->on && next_copy == 0) {
+        OOC_CUDA_TRY(cudaEventCreate(&prof->h2d0));
+        OOC_CUDA_TRY(cudaEventRecord(prof->h2d0, sc));
+      }
       OOC_CUDA_TRY(cudaMemcpy2DAsync(dst + c.c0, n * sizeof(double), src.A + c.c0 + c.c0 * src.lda,
                                      src.lda * sizeof(double), (n - c.c0) * sizeof(double), c.c1 - c.c0,
                                      cudaMemcpyHostToDevice, sc));
       OOC_CUDA_TRY(cudaEventRecord(evCopied[next_copy], sc));
+      prof->h2d_bytes += (double)(n - c.c0) * (double)(c.c1 - c.c0) * sizeof(double);
+      if (prof->on && next_copy == nchunks - 1) {
+        OOC_CUDA_TRY(cudaEventCreate(&prof->h2d1));
+        OOC_CUDA_TRY(cudaEventRecord(prof->h2d1, sc));
+      }
       next_copy++;
     }
     return OOC_OK;
@@ -2401,7 +2421,8 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     }
   }
   F->pool = ooc_handle_pool(h);
-  for (DevBuf* b : {&F->part, &F->partf, &F->work, &F->scratch, &F->work2, &F->part2}) b->pool = F->pool.get();
+  for (DevBuf* b : {&F->part, &F->partf, &F->work, &F->scratch, &F->work2, &F->part2, &F->rws, &F->sws})
+    b->pool = F->pool.get();
   int rc = alloc_factor(F, n, nb, reduced);
   if (rc) { delete F; return rc; }
   cudaEvent_t e0, e1;
@@ -2516,6 +2537,12 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     stats->npanels = 1;
     stats->info = st;
     stats->kernel_launches = launches;
+    stats->h2d_bytes = prof.h2d_bytes;
+    if (prof.h2d0 && prof.h2d1) {
+      float t = 0;
+      cudaEventElapsedTime(&t, prof.h2d0, prof.h2d1);
+      stats->h2d_ms = t;
+    }
     if (prof.on) {
       size_t fi = 0;
       for (size_t k = 0; k < prof.kind.size(); k++) {
@@ -2559,7 +2586,9 @@ extern "C" int ooc_factor_destroy(ooc_factor* F) {
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(F->device);
-  cudaDeviceSynchronize();
+  // No device-wide synchronisation: every call that used the factor waited for its own
+  // streams before returning, so its buffers are idle and go back to the handle's cache
+  // without stalling other pipelines' work.
   delete F;
   cudaSetDevice(prev);
   return OOC_OK;
@@ -2643,18 +2672,19 @@ extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t
   if (F->info != 0) return OOC_ERR_UNSUPPORTED;
   if (nrhs == 0) return OOC_OK;
   cudaSetDevice(F->device);
+  std::lock_guard<std::mutex> solve_lock(F->solve_mu);
   cudaStream_t s = ooc_compute_stream(h);
   const i64 n = F->n;
   int rc;
   if (F->Lf) {
-    DevBuf bf;
-    rc = bf.ensure((size_t)n * nrhs * sizeof(float));
+    rc = F->sws.ensure((size_t)n * RMAX * sizeof(float));
     if (rc) return rc;
+    float* bf = (float*)F->sws.p;
     const unsigned gb = (unsigned)((n + 255) / 256);
-    k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, (float*)bf.p, n, (int)n, nrhs);
-    rc = solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), (float*)bf.p, n, nrhs, F->tmpf, s, &F->partf);
-    if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>((const float*)bf.p, n, B, ldb, (int)n, nrhs);
-    if (!rc) rc = ooc_wait_stream(h, s);  // before the staging buffer goes
+    k_to_f32_cols<<<gb, 256, 0, s>>>(B, ldb, bf, n, (int)n, nrhs);
+    rc = solve_with<float>(F->Lf, n, F->Dinvf, F->panels(), bf, n, nrhs, F->tmpf, s, &F->partf);
+    if (!rc) k_f32_to_f64_cols<<<gb, 256, 0, s>>>((const float*)bf, n, B, ldb, (int)n, nrhs);
+    if (!rc) rc = ooc_wait_stream(h, s);
     return rc;
   }
   rc = solve_with<double>(F->L, n, F->Dinv, F->panels(), B, ldb, nrhs, F->tmp, s, &F->part);
@@ -2672,21 +2702,19 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
                        double alpha, const double* B, i64 ldb, double* X, i64 ldx, int r, double tol, int maxiter,
                        int* iters, double* berr) {
   cudaSetDevice(F->device);
+  std::lock_guard<std::mutex> solve_lock(F->solve_mu);
   cudaStream_t s = ooc_compute_stream(h);
   const i64 n = F->n;
-  double *R = nullptr, *red = nullptr, *rows = nullptr;
-  float* Rf = nullptr;
+  // the residual R (n x RMAX FP64), its FP32 copy, the row sums and the reduction words, in
+  // the factor's workspace (sized once for RMAX columns and kept across calls)
   const int nred = 152;
-  if (cudaMalloc(&R, (size_t)n * r * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&red, (size_t)nred * (r + 1) * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&rows, (size_t)n * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&Rf, (size_t)n * r * sizeof(float)) != cudaSuccess) {
-    cudaGetLastError();
-    if (R) cudaFree(R);
-    if (red) cudaFree(red);
-    if (rows) cudaFree(rows);
-    return OOC_ERR_NOMEM;
-  }
+  const size_t bR = (size_t)n * RMAX * sizeof(double), bRf = ((size_t)n * RMAX * sizeof(float) + 255) / 256 * 256;
+  const size_t bRows = ((size_t)n * sizeof(double) + 255) / 256 * 256;
+  if (F->rws.ensure(bR + bRf + bRows + (size_t)nred * (RMAX + 1) * sizeof(double))) return OOC_ERR_NOMEM;
+  double* R = (double*)F->rws.p;
+  float* Rf = (float*)((char*)F->rws.p + bR);
+  double* rows = (double*)((char*)F->rws.p + bR + bRf);
+  double* red = (double*)((char*)F->rws.p + bR + bRf + bRows);
   int rc = OOC_OK;
   // A given on the host: the lower triangle the factor kept (same pointer and lda), else
   // a device copy of the lower triangle, column block by column block.
@@ -2854,10 +2882,6 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
     cudaStreamSynchronize(s);
     F->release(Atmp);
   }
-  cudaFree(R);
-  cudaFree(red);
-  cudaFree(rows);
-  cudaFree(Rf);
   if (rc) return rc;
   if (iters) *iters = it;
   if (berr) *berr = be;

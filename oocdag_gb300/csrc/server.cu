@@ -32,9 +32,10 @@
 #include <vector>
 
 #include "common.cuh"
+#include "devpool.cuh"
 
 int ooc_batched_run_ptrs(cudaStream_t s, int dev, int count, double* const* a, double* const* b, const int* n,
-                         const int* mode, int* info_host, const int* blk_table);
+                         const int* mode, int* info_host, const int* blk_table, GrowBuf* ws);
 
 namespace {
 
@@ -129,12 +130,18 @@ struct ooc_server {
   std::vector<std::thread> workers;
   std::chrono::steady_clock::time_point t0;
   std::string last_error;
+  // Device memory in steady state comes from caches, so that a request never frees (a
+  // cudaFree synchronises the device under every other pipeline): small systems' factors
+  // from `small_pool` (kept by exact size), the batcher's right-hand sides, launch tables
+  // and per-system metadata from grow-only buffers.
+  std::shared_ptr<DevPool> small_pool;
+  GrowBuf bat_b, bat_meta, bat_ws;
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 
   void release_entry(Entry& e) {  // caller holds mu; device frees happen here
     if (e.F) ooc_factor_destroy(e.F);
-    if (e.Ls) cudaFree(e.Ls);
+    if (e.Ls) small_pool->release(e.Ls);
     e.F = nullptr;
     e.Ls = nullptr;
     resident -= e.bytes;
@@ -232,6 +239,7 @@ struct ooc_server {
     cudaSetDevice(cfg.device);
     ooc_handle* h = nullptr;
     if (ooc_create(&h, cfg.device) != OOC_OK) return;
+    GrowBuf wbuf;  // this pipeline's right-hand side and solution, kept across requests
     std::unique_lock<std::mutex> lk(mu);
     while (true) {
       cv_large.wait(lk, [&] { return stop || !large_q.empty(); });
@@ -254,9 +262,10 @@ struct ooc_server {
       }
       double *B = nullptr, *X = nullptr;
       if (status == OOC_OK && info == 0) {
-        if (cudaMalloc(&B, n * 8) != cudaSuccess || cudaMalloc(&X, n * 8) != cudaSuccess) {
-          cudaGetLastError();
-          status = OOC_ERR_NOMEM;
+        status = wbuf.ensure((size_t)n * 16);
+        if (status == OOC_OK) {
+          B = (double*)wbuf.p;
+          X = B + n;
         }
       }
       if (status == OOC_OK && info == 0) status = ooc_gen_normal(h, B, n, n, 1, j.r.rhs_seed);
@@ -267,8 +276,6 @@ struct ooc_server {
         if (cudaMemcpy(x.data(), X, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) status = OOC_ERR_CUDA;
         for (double v : x) xsum += v;
       }
-      if (B) cudaFree(B);
-      if (X) cudaFree(X);
       lk.lock();
       reserved -= j.reserve;
       if (j.hit) {
@@ -348,10 +355,12 @@ struct ooc_server {
     int status = OOC_OK;
     double* Bbuf = nullptr;
     void* meta = nullptr;
-    if (cudaMalloc(&Bbuf, std::max<int64_t>(btot, 1) * 8) != cudaSuccess ||
-        cudaMalloc(&meta, (size_t)count * (8 + 4 + 8 + 8 + 8 + 8) + 64) != cudaSuccess) {
-      cudaGetLastError();
+    if (bat_b.ensure((size_t)std::max<int64_t>(btot, 1) * 8) != OOC_OK ||
+        bat_meta.ensure((size_t)count * (8 + 4 + 8 + 8 + 8 + 8) + 64) != OOC_OK) {
       status = OOC_ERR_NOMEM;
+    } else {
+      Bbuf = (double*)bat_b.p;
+      meta = bat_meta.p;
     }
     int64_t off = 0;
     for (int i = 0; i < count && status == OOC_OK; i++) {
@@ -361,8 +370,8 @@ struct ooc_server {
         mode[i] = 1;
       } else {
         mode[i] = 0;
-        if (cudaMalloc(&Ls[i], (size_t)n[i] * n[i] * 8) != cudaSuccess) {
-          cudaGetLastError();
+        Ls[i] = (double*)small_pool->alloc((size_t)n[i] * n[i] * 8);
+        if (!Ls[i]) {
           status = OOC_ERR_NOMEM;
           break;
         }
@@ -400,7 +409,7 @@ struct ooc_server {
       chk(cudaGetLastError(), "k_fill_normals");
       if (status == OOC_OK)
         status = ooc_batched_run_ptrs(s, cfg.device, count, Ls.data(), b.data(), n.data(), mode.data(), info.data(),
-                                      nullptr);
+                                      nullptr, &bat_ws);
       if (status == OOC_OK) {
         k_small_berr<<<count, 256, 0, s>>>(d_b, d_n, d_ak, d_bk, count, d_be, d_xs);
         chk(cudaGetLastError(), "k_small_berr");
@@ -415,8 +424,6 @@ struct ooc_server {
         xs[i].resize(n[i]);
         cudaMemcpy(xs[i].data(), b[i], (size_t)n[i] * 8, cudaMemcpyDeviceToHost);
       }
-    if (Bbuf) cudaFree(Bbuf);
-    if (meta) cudaFree(meta);
     std::lock_guard<std::mutex> lk(mu);
     for (int i = 0; i < count; i++) {
       Job& j = batch[i];
@@ -444,7 +451,7 @@ struct ooc_server {
           made[i] = false;
         }
       }
-      if (made[i] && Ls[i]) cudaFree(Ls[i]);
+      if (made[i] && Ls[i]) small_pool->release(Ls[i]);  // not kept
       running--;
       complete(j, status, info[i], 0, 0, berr[i], xsum[i], &xs[i]);
     }
@@ -471,6 +478,9 @@ extern "C" int ooc_server_create(const ooc_server_config* cfg, ooc_server** out)
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   S->budget = S->cfg.hbm_budget > 0 ? S->cfg.hbm_budget : (int64_t)(fr / 10 * 9);
+  S->small_pool = std::make_shared<DevPool>();
+  S->small_pool->device = S->cfg.device;
+  S->small_pool->cap = (size_t)1 << 30;  // evicted small factors kept for reuse (2 MB each at n=512)
   S->t0 = std::chrono::steady_clock::now();
   S->sched = std::thread([S] { S->schedule_loop(); });
   S->batcher = std::thread([S] { S->batch_loop(); });
