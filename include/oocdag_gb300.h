@@ -127,6 +127,15 @@ int ooc_dpotrf_L(ooc_handle* h, double* A, int64_t n, int64_t lda, int nb, size_
 int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int nb, size_t dev_budget,
                  int* info, ooc_stats* stats);
 
+/* B := A^{-1} B with the lower factor L of A as ooc_dpotrf_L leaves it, host or device
+ * (ld ldl): the reference's VERIFY solve, dpotrs on the factored matrix
+ * (oocdag.cpp:436-439).  A host L is streamed through the device twice (forward and
+ * backward sweeps over nb-wide column panels, two panel buffers of n x nb doubles);
+ * dev_budget (0 = no limit) caps the device bytes, else OOC_ERR_BUDGET.  B: host or
+ * device, n x nrhs (ld ldb), nrhs <= 16, overwritten by the solution.                 */
+int ooc_dpotrs_L(ooc_handle* h, const double* L, int64_t n, int64_t ldl, int nb, size_t dev_budget, double* B,
+                 int64_t ldb, int nrhs);
+
 /* Drop-in for the reference driver entry (oocdag.cpp:18): same argument order, the
  * QUARK context replaced by an ooc_handle (NULL = a per-process handle on the current
  * device).  Returns the factorization time in seconds, or a negative status code.  */
@@ -237,6 +246,11 @@ typedef struct ooc_server_config {
   double tol;              /* backward-error target (default 1e-14)                      */
   double batch_window_ms;  /* the batcher waits this long for more small requests        */
   int64_t hbm_budget;      /* device bytes the server may hold (0 = 90% of free memory)  */
+  int64_t ooc_min_n;       /* new factors of order >= this are computed out of core: FP64
+                              ooc_dpotrf_L of a host-resident copy of the matrix through
+                              ooc_budget device bytes, solved with ooc_dpotrs_L (completion
+                              path 2), one at a time; <= 0 = never (every factor in HBM)  */
+  int64_t ooc_budget;      /* device panel budget of those factorizations (0 = 24 GiB)    */
 } ooc_server_config;
 typedef struct ooc_request {
   int kind;                /* 0: factor + solve, 1: solve with the factor resident under key */
@@ -250,7 +264,8 @@ typedef struct ooc_completion {
   int64_t id;
   int status;              /* OOC_OK or an error (OOC_ERR_BUDGET: never fits the budget) */
   int info;                /* LAPACK info                                                 */
-  int path;                /* 0: batched kernel, 1: factor + refinement pipeline          */
+  int path;                /* 0: batched kernel, 1: factor + refinement pipeline, 2: out
+                              of core (host-resident factor)                             */
   int factor_reused;       /* 1: solved with a resident factor                            */
   int iterations;          /* refinement steps                                            */
   double backward_error;   /* ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)           */

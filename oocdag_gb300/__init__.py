@@ -118,6 +118,7 @@ def load(build_if_missing: bool = True):
     L.ooc_last_info.argtypes = [P]
     L.ooc_dpotrf_L.argtypes = [P, P, I64, I64, I, SZ, ctypes.POINTER(I), ctypes.POINTER(OocStats)]
     L.ooc_spotrf_L.argtypes = [P, P, I64, I64, I, SZ, ctypes.POINTER(I), ctypes.POINTER(OocStats)]
+    L.ooc_dpotrs_L.argtypes = [P, P, I64, I64, I, SZ, P, I64, I]
     L.Cholesky.argtypes = [P, P, I, I, I, SZ]
     L.Cholesky.restype = D
     L.ooc_pdpotrf_.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), ctypes.POINTER(I),
@@ -254,6 +255,13 @@ class Handle:
         rc = load().ooc_dpotrf_L(self._h, _ptr(A), n, lda, nb, budget, ctypes.byref(info), ctypes.byref(st))
         _check(rc, "ooc_dpotrf_L")
         return Result(info.value, st.as_dict())
+
+    def dpotrs_L(self, L, n: int, ldl: int, nb: int, B, ldb: int, nrhs: int, budget: int = 0) -> None:
+        """B := A^{-1} B with the lower factor L (host or device, as dpotrf_L leaves it); a
+        host L is streamed through the device in nb-wide panels.  B (host or device) holds
+        nrhs <= 16 columns of leading dimension ldb."""
+        self._after_torch(L, B)
+        _check(load().ooc_dpotrs_L(self._h, _ptr(L), n, ldl, nb, budget, _ptr(B), ldb, nrhs), "ooc_dpotrs_L")
 
     def spotrf_L(self, A, n: int, lda: int, nb: int, budget: int = 0) -> Result:
         """FP32 lower Cholesky in place (device A: in place; host A: on a device copy that

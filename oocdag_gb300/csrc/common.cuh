@@ -124,6 +124,12 @@ struct GrowBuf {
 };
 // The handle's workspace for the batched solvers' launch tables.
 GrowBuf* ooc_handle_batch_ws(ooc_handle* h);
+// The handle's workspace for solves with a stored factor (ooc_dpotrs_L).
+GrowBuf* ooc_handle_solve_ws(ooc_handle* h);
+// Backward error of a solution x of A x = b (device vectors) for the uniform test matrix
+// of `seed` (mixed.cu), A regenerated on the fly.
+int ooc_seeded_backward_error(ooc_handle* h, int64_t n, uint64_t seed, double alpha, const double* B, const double* X,
+                              double* berr);
 
 // Generators (matgen.cu): fill the block of global rows [r0, r0+m) and columns
 // [c0, c0+nc) of the n x n test matrix into the device buffer B (leading dimension ldb).

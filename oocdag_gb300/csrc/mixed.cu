@@ -2694,6 +2694,172 @@ extern "C" int ooc_factor_solve(ooc_handle* h, ooc_factor* F, double* B, int64_t
 
 
 
+// B := A^{-1} B with the lower factor L of A as ooc_dpotrf_L leaves it (host or device,
+// ld ldl): the forward sweep L Y = B and the backward sweep L^T X = Y over nb-wide column
+// panels, each panel's inverse diagonal tile formed on the device (identity, then the
+// library's column solve: L_JJ^{-T}), then a small product with the panel below it.  A host
+// L is streamed: each sweep copies the panels' lower parts (rows J0..n-1) through two device
+// panel buffers on the host-to-device stream, the copy of the next panel beside the
+// compute of this one -- the dpotrs of the reference's VERIFY block (oocdag.cpp:436-439)
+// with the factor left where the out-of-core factorization put it.
+extern "C" int ooc_dpotrs_L(ooc_handle* h, const double* L, int64_t n, int64_t ldl, int nb, size_t dev_budget,
+                            double* B, int64_t ldb, int nrhs) {
+  if (!h) return -1;
+  if (!L && n > 0) return -2;
+  if (n < 0) return -3;
+  if (ldl < std::max<int64_t>(1, n)) return -4;
+  if (nb <= 0) return -5;
+  if (!B && n > 0) return -7;
+  if (ldb < std::max<int64_t>(1, n)) return -8;
+  if (nrhs < 0 || nrhs > RMAX) return -9;
+  if (n == 0 || nrhs == 0) return OOC_OK;
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  void* scp = nullptr;
+  ooc_get_stream(h, 1, &scp);
+  cudaStream_t sc = (cudaStream_t)scp;
+  auto on_device = [](const void* p) {
+    cudaPointerAttributes pa{};
+    const bool d = cudaPointerGetAttributes(&pa, p) == cudaSuccess &&
+                   (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    return d;
+  };
+  const bool l_dev = on_device(L), b_dev = on_device(B);
+  nb = (int)std::min<i64>(nb, n);
+  const int bb = (int)((n + nb - 1) / nb);
+  const i64 tile = (i64)nb * nb;
+  // workspace: status word, L_JJ^{-T}, nb x RMAX products, B's device copy, two panels
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t b_stat = 256, b_dinv = up(tile * 8), b_tmp = up((size_t)nb * RMAX * 8);
+  const size_t b_B = b_dev ? 0 : up((size_t)n * nrhs * 8), b_pan = l_dev ? 0 : up((size_t)n * nb * 8);
+  const size_t need = b_stat + b_dinv + b_tmp + b_B + 2 * b_pan;
+  if (dev_budget > 0 && need > dev_budget) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "ooc_dpotrs_L: n=%lld nb=%d needs %zu device bytes (two panels), budget %zu",
+             (long long)n, nb, need, dev_budget);
+    ooc_set_last_message(buf);
+    return OOC_ERR_BUDGET;
+  }
+  GrowBuf* ws = ooc_handle_solve_ws(h);
+  int rc = ws->ensure(need);
+  if (rc) return rc;
+  char* base = (char*)ws->p;
+  int* status = (int*)base;
+  double* D = (double*)(base + b_stat);
+  double* tmp = (double*)(base + b_stat + b_dinv);
+  double* Bd = b_dev ? B : (double*)(base + b_stat + b_dinv + b_tmp);
+  const i64 ldbd = b_dev ? ldb : n;
+  double* Pbuf[2] = {nullptr, nullptr};
+  if (!l_dev) {
+    Pbuf[0] = (double*)(base + b_stat + b_dinv + b_tmp + b_B);
+    Pbuf[1] = (double*)((char*)Pbuf[0] + b_pan);
+  }
+  struct EvGuard {  // copied (per slot), slot free (per slot), inputs ready
+    cudaEvent_t e[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~EvGuard() { for (cudaEvent_t x : e) if (x) cudaEventDestroy(x); }
+  } ev;
+  for (cudaEvent_t& x : ev.e) OOC_CUDA_TRY(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  cudaEvent_t* evc = ev.e;
+  cudaEvent_t* evf = ev.e + 2;
+  cudaEvent_t ev0 = ev.e[4];
+  OOC_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (!b_dev)
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(Bd, n * sizeof(double), B, ldb * sizeof(double), n * sizeof(double), nrhs,
+                                   cudaMemcpyHostToDevice, s));
+  OOC_CUDA_TRY(cudaEventRecord(ev0, s));
+  OOC_CUDA_TRY(cudaStreamWaitEvent(sc, ev0, 0));
+  auto panel_cols = [&](int J, i64* J0, int* LN) {
+    *J0 = (i64)J * nb;
+    *LN = (int)std::min<i64>(nb, n - *J0);
+  };
+  // panel J's lower part on the device: its address and leading dimension
+  auto fetch = [&](int J, int slot, int uses) -> int {  // uses: sweeps that used the slot before
+    if (l_dev) return OOC_OK;
+    i64 J0;
+    int LN;
+    panel_cols(J, &J0, &LN);
+    if (uses > 0) OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evf[slot], 0));
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(Pbuf[slot], n * sizeof(double), L + J0 + J0 * ldl, ldl * sizeof(double),
+                                   (n - J0) * sizeof(double), LN, cudaMemcpyHostToDevice, sc));
+    OOC_CUDA_TRY(cudaEventRecord(evc[slot], sc));
+    return OOC_OK;
+  };
+  int slot_uses[2] = {0, 0};
+  for (int sweep = 0; sweep < 2 && !rc; sweep++) {
+    // panel order: forward left to right, backward right to left
+    auto pj = [&](int t) { return sweep == 0 ? t : bb - 1 - t; };
+    if ((rc = fetch(pj(0), 0, slot_uses[0]))) break;
+    for (int t = 0; t < bb && !rc; t++) {
+      const int J = pj(t), slot = t % 2;
+      if (t + 1 < bb && (rc = fetch(pj(t + 1), (t + 1) % 2, slot_uses[(t + 1) % 2]))) break;
+      i64 J0;
+      int LN;
+      panel_cols(J, &J0, &LN);
+      const double* Pj;
+      i64 ldp;
+      if (l_dev) {
+        Pj = L + J0 + J0 * ldl;
+        ldp = ldl;
+      } else {
+        OOC_CUDA_TRY(cudaStreamWaitEvent(s, evc[slot], 0));
+        Pj = Pbuf[slot];
+        ldp = n;
+      }
+      const i64 rows = n - J0 - LN;
+      k_set_identity<double><<<dim3((LN + 255) / 256, std::min(LN, 1024)), 256, 0, s>>>(D, nb, LN);
+      rc = launch_trsm_col(Pj, ldp, TileCol{D, nb, tile}, 1, LN, LN, LN, status, s);  // D = L_JJ^{-T}
+      if (rc) break;
+      if (sweep == 0) {  // y_J = L_JJ^{-1} b_J, then b_below -= L_below y_J
+        if (nrhs == 1 && LN <= DMV_WARPS * 32) {
+          k_dinv_mv<double, true><<<(LN + 31) / 32, DMV_WARPS * 32, 0, s>>>(D, nb, LN, Bd + J0, tmp);
+          OOC_CUDA_TRY(cudaGetLastError());
+        } else if ((rc = gemm_tn_small<double, double>(D, nb, Bd + J0, ldbd, tmp, nb, LN, LN, nrhs, 1.0, 0.0, s))) {
+          break;
+        }
+        if (rows > 0) {
+          rc = gemm_nn_small<double, double>(Pj + LN, ldp, tmp, nb, Bd + J0 + LN, ldbd, (int)rows, LN, nrhs, -1.0, 1.0,
+                                             s, nullptr, CopyOut<double>{tmp, nb, Bd + J0, ldbd, LN});
+          if (rc) break;
+        } else {
+          OOC_CUDA_TRY(cudaMemcpy2DAsync(Bd + J0, ldbd * sizeof(double), tmp, nb * sizeof(double), LN * sizeof(double),
+                                         nrhs, cudaMemcpyDeviceToDevice, s));
+        }
+      } else {  // y_J -= L_below^T x_below, then x_J = L_JJ^{-T} y_J
+        if (rows > 0 && (rc = gemm_tn_small<double, double>(Pj + LN, ldp, Bd + J0 + LN, ldbd, Bd + J0, ldbd, LN,
+                                                            (int)rows, nrhs, -1.0, 1.0, s)))
+          break;
+        if (nrhs == 1 && LN <= DMV_WARPS * 32) {
+          k_dinv_mv<double, false><<<(LN + 31) / 32, DMV_WARPS * 32, 0, s>>>(D, nb, LN, Bd + J0, tmp);
+          OOC_CUDA_TRY(cudaGetLastError());
+        } else if ((rc = gemm_nn_small<double, double>(D, nb, Bd + J0, ldbd, tmp, nb, LN, LN, nrhs, 1.0, 0.0, s,
+                                                       nullptr))) {
+          break;
+        }
+        OOC_CUDA_TRY(cudaMemcpy2DAsync(Bd + J0, ldbd * sizeof(double), tmp, nb * sizeof(double), LN * sizeof(double),
+                                       nrhs, cudaMemcpyDeviceToDevice, s));
+      }
+      if (!l_dev) {
+        OOC_CUDA_TRY(cudaEventRecord(evf[slot], s));
+        slot_uses[slot]++;
+      }
+    }
+  }
+  if (!rc && !b_dev)
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(B, ldb * sizeof(double), Bd, n * sizeof(double), n * sizeof(double), nrhs,
+                                   cudaMemcpyDeviceToHost, s));
+  const int wrc = ooc_wait_stream(h, s);  // every queued use of the workspace is done
+  if (!rc) rc = wrc;
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      ooc_set_last_error(e, "ooc_dpotrs_L", __FILE__, __LINE__);
+      rc = OOC_ERR_CUDA;
+    }
+  }
+  return rc;
+}
+
 // Iterative refinement to a normwise backward error <= tol: X0 from the factor in FP64,
 // then repeat R = B - A X (FP64), D = A_F^{-1} R with the factor (FP32 copy for a
 // reduced-precision factor, FP64 otherwise), X += D.  A is either stored (Astore != null,
@@ -2885,6 +3051,49 @@ static int refine_impl(ooc_handle* h, ooc_factor* F, const double* Astore, i64 l
   if (rc) return rc;
   if (iters) *iters = it;
   if (berr) *berr = be;
+  return OOC_OK;
+}
+
+// Normwise backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) of one
+// solution x (device) of A x = b (device) for the uniform test matrix of `seed` and alpha,
+// with A regenerated inside the residual and the norm (no copy of A).  For solutions
+// computed without a factor object (the out-of-core path of the serving runtime).
+int ooc_seeded_backward_error(ooc_handle* h, int64_t n, uint64_t seed, double alpha, const double* B, const double* X,
+                              double* berr) {
+  cudaSetDevice(ooc_device(h));
+  cudaStream_t s = ooc_compute_stream(h);
+  const uint64_t key = ooc_uniform_key(seed);
+  const unsigned gb = (unsigned)((n + 255) / 256);
+  const int gslices = std::max(1, std::min((int)((n + 1023) / 1024), (int)((4 * 304 + gb - 1) / gb)));
+  const int gks = (int)((n + gslices - 1) / gslices);
+  const int nred = 152;
+  GrowBuf* ws = ooc_handle_solve_ws(h);
+  const size_t bvec = ((size_t)n * 8 + 255) / 256 * 256;
+  int rc = ws->ensure(2 * bvec + (size_t)gslices * n * 8 + (size_t)nred * 3 * 8);
+  if (rc) return rc;
+  double* R = (double*)ws->p;
+  double* rows = (double*)((char*)ws->p + bvec);
+  double* part = (double*)((char*)ws->p + 2 * bvec);
+  double* red = part + (size_t)gslices * n;
+  k_residual_init<<<gb, 256, 0, s>>>(B, n, R, n, (int)n, 1);
+  k_resid_gen<1><<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, X, n, 1, gks, part);
+  k_reduce_slices<double><<<gb, 256, 0, s>>>(part, gslices, R, n, (int)n, 1, -1.0, 1.0);
+  k_rowsum_gen<<<dim3(gb, gslices), 256, 0, s>>>(key, n, alpha, gks, part);
+  k_sum_slices_rows<<<gb, 256, 0, s>>>(part, gslices, n, rows);
+  k_colmax_abs<<<nred, 256, 0, s>>>(R, n, (int)n, 1, red);
+  k_colmax_abs<<<nred, 256, 0, s>>>(X, n, (int)n, 1, red + nred);
+  k_colmax_abs<<<nred, 256, 0, s>>>(B, n, (int)n, 1, red + 2 * nred);
+  k_colmax_abs<<<nred, 256, 0, s>>>(rows, n, (int)n, 1, red + 3 * nred);
+  OOC_CUDA_TRY(cudaGetLastError());
+  std::vector<double> hv((size_t)nred * 4);
+  OOC_CUDA_TRY(cudaMemcpyAsync(hv.data(), red, hv.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  rc = ooc_wait_stream(h, s);
+  if (rc) return rc;
+  double m[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; k++)
+    for (int b = 0; b < nred; b++) m[k] = std::max(m[k], hv[(size_t)k * nred + b]);
+  const double den = m[3] * m[1] + m[2];
+  *berr = den > 0 ? m[0] / den : 0.0;
   return OOC_OK;
 }
 

@@ -73,6 +73,7 @@ struct ooc_handle {
   int64_t block_cols = -1;  // OOC_OPT_BLOCK_COLS (-1: by input)
   std::shared_ptr<DevPool> pool;  // device buffers of the handle's factor objects
   GrowBuf batch_ws;               // launch tables of the batched solvers
+  GrowBuf solve_ws;               // panels and vectors of ooc_dpotrs_L
   int last_info = 0;
   std::vector<cudaEvent_t> ev_pool;  // reusable timing-free events
   size_t ev_next = 0;
@@ -177,6 +178,7 @@ extern "C" int ooc_create(ooc_handle** out, int device) {
 
 std::shared_ptr<DevPool> ooc_handle_pool(ooc_handle* h) { return h ? h->pool : nullptr; }
 GrowBuf* ooc_handle_batch_ws(ooc_handle* h) { return h ? &h->batch_ws : nullptr; }
+GrowBuf* ooc_handle_solve_ws(ooc_handle* h) { return h ? &h->solve_ws : nullptr; }
 
 extern "C" int ooc_destroy(ooc_handle* h) {
   if (!h) return OOC_OK;
@@ -190,6 +192,7 @@ extern "C" int ooc_destroy(ooc_handle* h) {
     if (h->ev_wait) cudaEventDestroy(h->ev_wait);
     if (h->d_buf) cudaFree(h->d_buf);
     h->batch_ws.release();
+    h->solve_ws.release();
     if (h->d_status) cudaFree(h->d_status);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->s_h2d) cudaStreamDestroy(h->s_h2d);

@@ -97,6 +97,7 @@ struct Job {
   int64_t reserve = 0;       // bytes reserved at admission
   int64_t factor_bytes = 0;  // part of `reserve` that stays resident afterwards
   bool small = false;
+  bool ooc = false;          // factored out of core (host-resident matrix, capped device budget)
   bool hit = false;          // solved with a resident factor
 };
 
@@ -200,14 +201,19 @@ struct ooc_server {
         j.small = j.r.n <= cfg.small_max_n;
         auto it = cache.find(j.r.key);
         const bool hit = j.r.kind == 1 && it != cache.end() && it->second.n == j.r.n && (it->second.F || it->second.Ls);
+        j.ooc = !hit && !j.small && cfg.ooc_min_n > 0 && j.r.n >= cfg.ooc_min_n;
         const int64_t n = j.r.n;
-        const int64_t need_f = hit ? 0 : (j.small ? 8 * n * n : ooc_factor_bytes(n, cfg.nb, cfg.prec));
-        const int64_t need_w = j.small ? 64 * n : 64 * n + (64LL << 20);
+        // out of core: the factor lives in host memory; the device holds the panel budget
+        // and the solve's two panels
+        const int64_t need_f = hit || j.ooc ? 0 : (j.small ? 8 * n * n : ooc_factor_bytes(n, cfg.nb, cfg.prec));
+        const int64_t need_w = j.small ? 64 * n
+                               : j.ooc ? cfg.ooc_budget + 16 * n * cfg.nb + 64 * n + (64LL << 20)
+                                       : 64 * n + (64LL << 20);
         const int64_t need = need_f + need_w;
         if (need > budget) {  // can never fit this device budget
           Job jj = j;
           pending.erase(pending.begin() + i);
-          complete(jj, OOC_ERR_BUDGET, 0, jj.small ? 0 : 1, 0, 0.0, 0.0, nullptr);
+          complete(jj, OOC_ERR_BUDGET, 0, jj.small ? 0 : jj.ooc ? 2 : 1, 0, 0.0, 0.0, nullptr);
           continue;
         }
         if (!evict_for(need, hit ? j.r.key : -1)) {
@@ -234,6 +240,61 @@ struct ooc_server {
     }
   }
 
+  // ---------------------------------------------------------------- out of core
+  // FP64 factorization of a host-resident copy of the matrix through cfg.ooc_budget device
+  // bytes (ooc_dpotrf_L, the reference's panel streaming), the solve with the host factor
+  // (ooc_dpotrs_L) and the backward error with A regenerated on the device.  One at a time
+  // (they share the server's page-locked host matrix, grown to the largest order seen); the
+  // host factor is not kept, so a repeat solve of such a key factors again.
+  std::mutex ooc_mu;
+  double* ooc_host = nullptr;
+  size_t ooc_host_bytes = 0;
+  void run_ooc(ooc_handle* h, const Job& j, GrowBuf& wbuf) {
+    const int64_t n = j.r.n;
+    const double alpha = (double)n;
+    int status = OOC_OK, info = 0;
+    double berr = 0, xsum = 0;
+    std::vector<double> x;
+    {
+      std::lock_guard<std::mutex> olk(ooc_mu);
+      const size_t bytes = (size_t)n * n * sizeof(double);
+      if (ooc_host_bytes < bytes) {
+        if (ooc_host) cudaFreeHost(ooc_host);
+        ooc_host = nullptr;
+        ooc_host_bytes = 0;
+        if (cudaHostAlloc((void**)&ooc_host, bytes, cudaHostAllocDefault) != cudaSuccess) {
+          cudaGetLastError();
+          ooc_host = nullptr;
+          status = OOC_ERR_NOMEM;
+        } else {
+          ooc_host_bytes = bytes;
+        }
+      }
+      if (status == OOC_OK) status = ooc_dmatgen_uniform(h, ooc_host, n, n, j.r.matrix_seed, alpha);
+      if (status == OOC_OK)
+        status = ooc_dpotrf_L(h, ooc_host, n, n, cfg.nb, (size_t)cfg.ooc_budget, &info, nullptr);
+      double *B = nullptr, *X = nullptr;
+      if (status == OOC_OK && info == 0 && (status = wbuf.ensure((size_t)n * 16)) == OOC_OK) {
+        B = (double*)wbuf.p;
+        X = B + n;
+        status = ooc_gen_normal(h, B, n, n, 1, j.r.rhs_seed);
+        if (status == OOC_OK && cudaMemcpy(X, B, (size_t)n * 8, cudaMemcpyDeviceToDevice) != cudaSuccess)
+          status = OOC_ERR_CUDA;
+        if (status == OOC_OK) status = ooc_dpotrs_L(h, ooc_host, n, n, cfg.nb, 0, X, n, 1);
+        if (status == OOC_OK) status = ooc_seeded_backward_error(h, n, j.r.matrix_seed, alpha, B, X, &berr);
+        if (status == OOC_OK) {
+          x.resize(n);
+          if (cudaMemcpy(x.data(), X, (size_t)n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) status = OOC_ERR_CUDA;
+          for (double v : x) xsum += v;
+        }
+      }
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    reserved -= j.reserve;
+    running--;
+    complete(j, status, info, 2, 0, berr, xsum, &x);
+  }
+
   // ---------------------------------------------------------------- large requests
   void worker_loop() {
     cudaSetDevice(cfg.device);
@@ -250,6 +311,11 @@ struct ooc_server {
       ooc_factor* F = nullptr;
       if (j.hit) F = cache[j.r.key].F;
       lk.unlock();
+      if (j.ooc) {
+        run_ooc(h, j, wbuf);
+        lk.lock();
+        continue;
+      }
       const int64_t n = j.r.n;
       const double alpha = (double)n;
       int status = OOC_OK, info = 0, iters = 0;
@@ -478,6 +544,7 @@ extern "C" int ooc_server_create(const ooc_server_config* cfg, ooc_server** out)
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   S->budget = S->cfg.hbm_budget > 0 ? S->cfg.hbm_budget : (int64_t)(fr / 10 * 9);
+  if (S->cfg.ooc_budget <= 0) S->cfg.ooc_budget = 24LL << 30;
   S->small_pool = std::make_shared<DevPool>();
   S->small_pool->device = S->cfg.device;
   S->small_pool->cap = (size_t)1 << 30;  // evicted small factors kept for reuse (2 MB each at n=512)
@@ -566,6 +633,7 @@ extern "C" int ooc_server_destroy(ooc_server* S) {
   cudaSetDevice(S->cfg.device);
   for (auto& kv : S->cache) S->release_entry(kv.second);
   S->cache.clear();
+  if (S->ooc_host) cudaFreeHost(S->ooc_host);
   delete S;
   return OOC_OK;
 }

@@ -13,7 +13,8 @@ from . import OocError, PRECISIONS, load
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("workers", ctypes.c_int), ("small_max_n", ctypes.c_int),
                 ("nb", ctypes.c_int), ("prec", ctypes.c_int), ("tol", ctypes.c_double),
-                ("batch_window_ms", ctypes.c_double), ("hbm_budget", ctypes.c_int64)]
+                ("batch_window_ms", ctypes.c_double), ("hbm_budget", ctypes.c_int64),
+                ("ooc_min_n", ctypes.c_int64), ("ooc_budget", ctypes.c_int64)]
 
 
 class Request(ctypes.Structure):
@@ -56,9 +57,9 @@ def _lib():
 
 class Server:
     def __init__(self, device=0, workers=4, small_max_n=512, nb=512, prec="bf16x3", tol=1e-14,
-                 batch_window_ms=0.5, hbm_budget=0):
+                 batch_window_ms=0.5, hbm_budget=0, ooc_min_n=0, ooc_budget=0):
         cfg = ServerConfig(device, workers, small_max_n, nb, PRECISIONS[prec] if isinstance(prec, str) else prec,
-                           tol, batch_window_ms, hbm_budget)
+                           tol, batch_window_ms, hbm_budget, ooc_min_n, ooc_budget)
         p = ctypes.c_void_p()
         rc = _lib().ooc_server_create(ctypes.byref(cfg), ctypes.byref(p))
         if rc:

@@ -107,6 +107,7 @@ def test_every_entry_point_checks_its_handle_first(ooc):
     assert L.ooc_get_option(None, ooc.OPT_TAIL_ORDER, b(v)) == -1
     assert L.ooc_last_info(None) == 0
     assert L.ooc_destroy(None) == ooc.OOC_OK
+    assert L.ooc_dpotrs_L(None, buf, 4, 4, 4, 0, buf, 4, 1) == -1
     assert L.ooc_dpotrf_L_static(None, 10, 10, 4, None, b(info)) == -1  # NULL matrix, n > 0
     S = server._lib()
     cnt, p64 = ctypes.c_int(0), ctypes.c_int64(0)

@@ -250,3 +250,47 @@ def test_profile_stats(oracle_mod, handle, ooc):
 def test_fp64_peak_probe(handle):
     tf = handle.fp64_peak(50.0)
     assert 0.3 < tf < 5.0
+
+
+@pytest.mark.parametrize("where,nrhs,nb", [("host", 1, 256), ("host", 16, 128), ("device", 3, 200)])
+def test_solve_with_the_out_of_core_factor(oracle_mod, handle, where, nrhs, nb):
+    """ooc_dpotrs_L: the reference's VERIFY solve (dpotrs on the factored matrix,
+    oocdag.cpp:436-439) with the factor left by the out-of-core factorization -- a host L
+    streamed through the device panel by panel, or a device L -- against LAPACK dpotrs on
+    the oracle's factor."""
+    import torch
+
+    n = 2900
+    A = oracle_mod.gen_uniform(n, 31, float(n))
+    tiles = 3 * ((n + nb - 1) // nb) + 6  # a few panels
+    Lh = A.copy(order="F")
+    r = handle.dpotrf_L(Lh, n, n, nb, tiles * nb * nb * 8)
+    assert r.info == 0 and r.stats["npanels"] >= 2
+    Lo, _ = _oracle_factor(oracle_mod, A, nb, tiles)
+    B = np.asfortranarray(np.random.default_rng(nrhs).standard_normal((n, nrhs)))
+    Xo = oracle_mod.potrs(Lo, B)
+    if where == "host":
+        X = B.copy(order="F")
+        handle.dpotrs_L(Lh, n, n, nb, X, n, nrhs, budget=2 * n * nb * 8 + (8 << 20))
+    else:
+        Ld = _to_dev(Lh)
+        Xd = _to_dev(B)
+        handle.dpotrs_L(Ld, n, n, nb, Xd, n, nrhs)
+        X = _from_dev(Xd)
+    assert np.abs(X - Xo).max() / np.abs(Xo).max() < 1e-12
+
+    def berr(Y):  # normwise backward error, worst column
+        nA = np.abs(A).sum(axis=1).max()
+        return max(np.abs(B[:, q] - A @ Y[:, q]).max() / (nA * np.abs(Y[:, q]).max() + np.abs(B[:, q]).max())
+                   for q in range(nrhs))
+
+    assert berr(X) <= 1e-14 and berr(X) <= 10 * berr(Xo) + 1e-16, (berr(X), berr(Xo))
+
+
+def test_out_of_core_solve_rejects_a_small_budget(oracle_mod, handle, ooc):
+    n, nb = 1000, 128
+    L = np.asfortranarray(np.eye(n))
+    B = np.asfortranarray(np.ones((n, 1)))
+    with pytest.raises(ooc.OocError) as e:
+        handle.dpotrs_L(L, n, n, nb, B, n, 1, budget=n * nb * 8)
+    assert e.value.code == ooc.OOC_ERR_BUDGET

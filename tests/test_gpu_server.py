@@ -29,12 +29,20 @@ def _mix():
     rng = np.random.default_rng(3)
     reqs = []
     for i in range(40):
-        n = int(np.exp(rng.uniform(np.log(64), np.log(3000))))
+        n = int(np.exp(rng.uniform(np.log(64), np.log(2400))))
         reqs.append(dict(n=n, matrix_seed=1000 + i, rhs_seed=5000 + i, key=i, kind=0))
+    # two systems routed out of core (order >= OOC_MIN_N): FP64 factor of a host copy
+    # through a small device budget, solve with the host factor
+    reqs.append(dict(n=2600, matrix_seed=777, rhs_seed=778, key=100, kind=0))
+    reqs.append(dict(n=2900, matrix_seed=779, rhs_seed=780, key=101, kind=0))
     # repeat solves on some of the matrices, fresh right-hand sides
     for k, i in enumerate([0, 3, 7, 11, 20, 31]):
         reqs.append(dict(n=reqs[i]["n"], matrix_seed=1000 + i, rhs_seed=9000 + k, key=i, kind=1))
     return reqs
+
+
+# the out-of-core route in these tests: orders from 2500, a device panel budget of 40 tiles
+OOC = dict(ooc_min_n=2500, ooc_budget=40 * 256 * 256 * 8)
 
 
 def test_mix_equals_alone_and_reaches_tolerance(ooc):
@@ -43,19 +51,19 @@ def test_mix_equals_alone_and_reaches_tolerance(ooc):
     reqs = _mix()
     # alone: one request at a time (each waits for the previous to finish)
     alone = {}
-    with Server(workers=4, nb=256, prec="bf16x3", batch_window_ms=0.2) as S:
+    with Server(workers=4, nb=256, prec="bf16x3", batch_window_ms=0.2, **OOC) as S:
         for q in reqs:
             rid = S.submit(keep_solution=True, **q)
             c = _drain(S, [rid])[rid]
             assert c["status"] == 0 and c["info"] == 0, (c, S.last_error())
             alone[(q["key"], q["rhs_seed"])] = (S.solution(rid, q["n"]), c)
     # mix: everything submitted at once; small ones batch together, large ones overlap
-    with Server(workers=4, nb=256, prec="bf16x3", batch_window_ms=2.0) as S:
+    with Server(workers=4, nb=256, prec="bf16x3", batch_window_ms=2.0, **OOC) as S:
         ids = {}
-        for q in reqs[:40]:
+        for q in reqs[:42]:
             ids[S.submit(keep_solution=True, **q)] = q
         first = _drain(S, list(ids))
-        for q in reqs[40:]:  # repeats after their factors exist
+        for q in reqs[42:]:  # repeats after their factors exist
             ids[S.submit(keep_solution=True, **q)] = q
         rest = _drain(S, [i for i in ids if i not in first])
         done = {**first, **rest}
@@ -69,7 +77,7 @@ def test_mix_equals_alone_and_reaches_tolerance(ooc):
             if q["kind"] == 1:
                 assert c["factor_reused"] == 1
         paths = {c["path"] for c in done.values()}
-        assert paths == {0, 1}  # both the batched kernel and the pipelines were used
+        assert paths == {0, 1, 2}  # the batched kernel, the pipelines and the out-of-core route
 
 
 def test_refuses_requests_that_never_fit(ooc):
