@@ -122,8 +122,11 @@ int ooc_dpotrf_L(ooc_handle* h, double* A, int64_t n, int64_t lda, int nb, size_
 /* FP32 Cholesky A = L L^T in place (lower; upper triangle untouched).  The reference has
  * no FP32 entry (LIN/psmatgen.f exists but nothing binds it).  A on the device: factored
  * in place (FP32 diagonal tiles, column solves and FP32 trailing updates, nb <= 512).
- * A on the host: factored on a device copy, which must fit in dev_budget bytes (0 = 3/4
- * of free device memory), else OOC_ERR_BUDGET.  *info as for ooc_dpotrf_L.            */
+ * A on the host: on a device copy when it fits dev_budget bytes (0 = 3/4 of free device
+ * memory); otherwise out of core, left-looking over panels of W columns with
+ * 3 n W floats <= dev_budget (the panel and two buffers of earlier columns streamed from
+ * the host, oocdag.cpp:59-87), OOC_ERR_BUDGET if not even W = nb fits.
+ * *info as for ooc_dpotrf_L.                                                          */
 int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int nb, size_t dev_budget,
                  int* info, ooc_stats* stats);
 
@@ -148,6 +151,13 @@ double Cholesky(void* handle, double* A, int N, int NB, int LDA, size_t memsize)
  * OOC_DEVICE_BUDGET_MB environment variable, else 3/4 of free device memory.      */
 void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const int* ia, const int* ja,
                   const int* desca, int* info);
+
+/* FP32 ScaLAPACK-style entry (pspotrf_ argument order, same descriptor and budget rules as
+ * ooc_pdpotrf_): ooc_spotrf_L on the sub-matrix; a host matrix larger than the budget is
+ * factored out of core.  No FP32 entry exists in the reference; this mirrors its
+ * descriptor form for the single-precision ScaLAPACK routine.                         */
+void ooc_pspotrf_(const char* uplo, const int* n, float* a, const int* ia, const int* ja, const int* desca,
+                  int* info);
 
 /* Panel plan of the left-looking loop: writes (jb, Ym, Yn) triples for an n x n matrix,
  * tile nb and a budget of memBlock tiles, counting nx X buffers (nx = 1 reproduces

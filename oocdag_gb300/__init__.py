@@ -124,6 +124,9 @@ def load(build_if_missing: bool = True):
     L.ooc_pdpotrf_.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), ctypes.POINTER(I),
                                ctypes.POINTER(I), ctypes.POINTER(I)]
     L.ooc_pdpotrf_.restype = None
+    L.ooc_pspotrf_.argtypes = [ctypes.c_char_p, ctypes.POINTER(I), P, ctypes.POINTER(I), ctypes.POINTER(I),
+                               ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.ooc_pspotrf_.restype = None
     L.ooc_dmatgen_pdmatgen.argtypes = [P, P, I64, I64, I]
     L.ooc_dmatgen_uniform.argtypes = [P, P, I64, I64, U64, D]
     L.ooc_dresidual.argtypes = [P, P, I64, I64, I, U64, D, ctypes.POINTER(D)]
@@ -369,6 +372,17 @@ def pdpotrf(uplo: str, n: int, A, ia: int, ja: int, desca) -> int:
     d = (ctypes.c_int * 9)(*[int(x) for x in desca])
     info = ctypes.c_int(0)
     L.ooc_pdpotrf_(uplo.encode(), ctypes.byref(ctypes.c_int(n)), _ptr(A), ctypes.byref(ctypes.c_int(ia)),
+                   ctypes.byref(ctypes.c_int(ja)), d, ctypes.byref(info))
+    return info.value
+
+
+def pspotrf(uplo: str, n: int, A, ia: int, ja: int, desca) -> int:
+    """ScaLAPACK-style pspotrf_ (FP32) on a 1x1 grid; returns info.  The device budget is
+    the OOC_DEVICE_BUDGET_MB environment variable, else 3/4 of free device memory."""
+    L = load()
+    d = (ctypes.c_int * 9)(*[int(x) for x in desca])
+    info = ctypes.c_int(0)
+    L.ooc_pspotrf_(uplo.encode(), ctypes.byref(ctypes.c_int(n)), _ptr(A), ctypes.byref(ctypes.c_int(ia)),
                    ctypes.byref(ctypes.c_int(ja)), d, ctypes.byref(info))
     return info.value
 

@@ -3184,6 +3184,150 @@ extern "C" int ooc_dsyrk_ln(ooc_handle* h, int prec, int n, int k, const double*
 // reduced-precision factor pipeline with FP32 trailing updates (k_syrk_f32), on the
 // matrix itself (device) or on a device copy of it (host, when it fits in dev_budget).
 // ---------------------------------------------------------------------------------
+namespace {
+// FP32 lower Cholesky of a HOST matrix through `budget` device bytes: the reference's
+// left-looking panel loop (oocdag.cpp:59-87) with panels of W columns (W from the budget:
+// the panel and two copies of earlier columns, each n x W floats).  Per panel, on the
+// compute stream s: the panel's lower part arrives (copy stream sc), every earlier panel's
+// columns arrive W at a time through two X buffers and update it (FP32 k_syrk_f32 restricted
+// to the panel's columns: the A2X + ooc_syrk tasks, oocquark.cpp:301-356), then the panel is
+// factored in core right-looking (FP32 diagonal tile, column solve, updates inside the
+// panel: ooc_incore, oocquark.cpp:358-421) and copied back (stream sd) before any later
+// panel reads its columns from the host.
+int spotrf_host_ooc(ooc_handle* h, float* A, i64 n, i64 lda, int nb, size_t budget, int* info, ooc_stats* stats) {
+  const i64 W = (i64)(budget / ((size_t)3 * n * sizeof(float))) / nb * nb;
+  if (W < nb) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "ooc_spotrf_L: budget %zu bytes below one panel (3 n nb floats = %zu)", budget,
+             (size_t)3 * n * nb * sizeof(float));
+    ooc_set_last_message(buf);
+    return OOC_ERR_BUDGET;
+  }
+  cudaStream_t s = ooc_compute_stream(h);
+  void *p1 = nullptr, *p2 = nullptr;
+  ooc_get_stream(h, 1, &p1);
+  ooc_get_stream(h, 2, &p2);
+  cudaStream_t sc = (cudaStream_t)p1, sd = (cudaStream_t)p2;
+  auto pool = ooc_handle_pool(h);
+  DevBuf Pb, Xb[2], work, aux;
+  for (DevBuf* b : {&Pb, &Xb[0], &Xb[1], &work, &aux}) b->pool = pool.get();
+  const i64 tile = (i64)nb * nb;
+  int rc;
+  if ((rc = Pb.ensure((size_t)n * W * sizeof(float))) || (rc = Xb[0].ensure((size_t)n * W * sizeof(float))) ||
+      (rc = Xb[1].ensure((size_t)n * W * sizeof(float))) ||
+      (rc = aux.ensure((size_t)2 * tile * sizeof(float) + 256)))
+    return rc;
+  float* P = (float*)Pb.p;
+  float* Dinv = (float*)aux.p;      // the diagonal kernel's inverse output (not kept)
+  float* Xr = Dinv + tile;          // L_jj^{-1}, row-major, for the column solve
+  int* status = (int*)(Xr + tile);
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DG_SMEM));
+  OOC_CUDA_TRY(cudaFuncSetAttribute(k_diag_s256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DS_SMEM));
+  struct Ev {
+    cudaEvent_t e[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~Ev() { for (cudaEvent_t x : e) if (x) cudaEventDestroy(x); }
+  } ev;
+  for (cudaEvent_t& x : ev.e) OOC_CUDA_TRY(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  cudaEvent_t evPin = ev.e[0], evPdone = ev.e[1], evPfree = ev.e[2], evXin[2] = {ev.e[3], ev.e[4]},
+              evXfree[2] = {ev.e[5], ev.e[6]};
+  cudaEvent_t t0, t1;
+  OOC_CUDA_TRY(cudaEventCreate(&t0));
+  OOC_CUDA_TRY(cudaEventCreate(&t1));
+  struct T2 {
+    cudaEvent_t a, b;
+    ~T2() { cudaEventDestroy(a); cudaEventDestroy(b); }
+  } tguard{t0, t1};
+  OOC_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+  OOC_CUDA_TRY(cudaEventRecord(t0, s));
+  OOC_CUDA_TRY(cudaEventRecord(evPfree, s));  // the panel buffer is free
+  int xuses[2] = {0, 0}, xslot = 0;
+  double h2d = 0, d2h = 0;
+  int64_t launches = 0;
+  int npanels = 0;
+  for (i64 J0 = 0; J0 < n; J0 += W, npanels++) {
+    const i64 Wp = std::min(W, n - J0), m = n - J0;
+    // the panel's lower part (A2Y)
+    OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evPfree, 0));
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(P, n * sizeof(float), A + J0 + J0 * lda, lda * sizeof(float), m * sizeof(float),
+                                   Wp, cudaMemcpyHostToDevice, sc));
+    OOC_CUDA_TRY(cudaEventRecord(evPin, sc));
+    h2d += (double)m * Wp * 4;
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s, evPin, 0));
+    const int bjp = (int)((Wp + 127) / 128);
+    // left-looking: the finished columns [K0, K0 + Kw), rows J0..n-1 (A2X + ooc_syrk)
+    for (i64 K0 = 0; K0 < J0; K0 += W) {
+      const i64 Kw = std::min(W, J0 - K0);
+      const int sl = xslot;
+      xslot ^= 1;
+      if (xuses[sl]) OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evXfree[sl], 0));
+      float* X = (float*)Xb[sl].p;
+      OOC_CUDA_TRY(cudaMemcpy2DAsync(X, n * sizeof(float), A + J0 + K0 * lda, lda * sizeof(float), m * sizeof(float),
+                                     Kw, cudaMemcpyHostToDevice, sc));
+      OOC_CUDA_TRY(cudaEventRecord(evXin[sl], sc));
+      h2d += (double)m * Kw * 4;
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s, evXin[sl], 0));
+      if ((rc = syrk_f32(OOC_PREC_FP32, X, n, P, n, (int)m, (int)Kw, status, s, work, 0, bjp))) return rc;
+      OOC_CUDA_TRY(cudaEventRecord(evXfree[sl], s));
+      xuses[sl]++;
+      launches++;
+    }
+    // in-core factorization of the panel, right-looking inside it (ooc_incore)
+    for (i64 q0 = 0; q0 < Wp; q0 += nb) {
+      const int LN = (int)std::min<i64>(nb, Wp - q0);
+      float* Djj = P + q0 + q0 * n;
+      if (LN <= DS_MAX)
+        k_diag_s256<<<1, DG_THREADS, DS_SMEM, s>>>(Djj, n, LN, J0 + q0, Dinv, LN, Xr, nullptr, nullptr, status);
+      else
+        k_diag_f32<<<1, DG_THREADS, DG_SMEM, s>>>(Djj, n, LN, J0 + q0, Dinv, LN, Xr, nullptr, nullptr, status);
+      OOC_CUDA_TRY(cudaGetLastError());
+      const i64 mq = m - q0 - LN;
+      launches++;
+      if (mq <= 0) continue;
+      float* Pn = Djj + LN;
+      k_colsolve_f32<<<(unsigned)((mq + CS_ROWS - 1) / CS_ROWS), FTHR, 0, s>>>(Pn, n, Xr, LN, (int)mq, LN, status);
+      OOC_CUDA_TRY(cudaGetLastError());
+      launches++;
+      const i64 wrest = Wp - q0 - LN;  // the panel's columns right of this step
+      if (wrest > 0) {
+        if ((rc = syrk_f32(OOC_PREC_FP32, Pn, n, Pn + LN * n, n, (int)mq, LN, status, s, work, 0,
+                           (int)((wrest + 127) / 128))))
+          return rc;
+        launches++;
+      }
+    }
+    // the factored panel back to the host (Y2A), before later panels read its columns
+    OOC_CUDA_TRY(cudaEventRecord(evPdone, s));
+    OOC_CUDA_TRY(cudaStreamWaitEvent(sd, evPdone, 0));
+    OOC_CUDA_TRY(cudaMemcpy2DAsync(A + J0 + J0 * lda, lda * sizeof(float), P, n * sizeof(float), m * sizeof(float), Wp,
+                                   cudaMemcpyDeviceToHost, sd));
+    OOC_CUDA_TRY(cudaEventRecord(evPfree, sd));
+    d2h += (double)m * Wp * 4;
+  }
+  OOC_CUDA_TRY(cudaStreamWaitEvent(s, evPfree, 0));
+  OOC_CUDA_TRY(cudaEventRecord(t1, s));
+  int st = 0;
+  if ((rc = read_int(status, &st, s))) return rc;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    ooc_set_last_error(e, "ooc_spotrf_L (out of core)", __FILE__, __LINE__);
+    return OOC_ERR_CUDA;
+  }
+  *info = st;
+  if (stats) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t0, t1);
+    stats->seconds = ms * 1e-3;
+    stats->flops = (double)n * n * n / 3.0;
+    stats->npanels = npanels;
+    stats->info = st;
+    stats->kernel_launches = launches;
+    stats->h2d_bytes = h2d;
+    stats->d2h_bytes = d2h;
+  }
+  return OOC_OK;
+}
+}  // namespace
+
 extern "C" int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int nb, size_t dev_budget, int* info,
                             ooc_stats* stats) {
   if (!h) return -1;
@@ -3218,10 +3362,8 @@ extern "C" int ooc_spotrf_L(ooc_handle* h, float* A, int64_t n, int64_t lda, int
       cudaMemGetInfo(&fr, &tot);
       budget = fr / 4 * 3;
     }
-    if (bytes > budget) {
-      ooc_set_last_message("ooc_spotrf_L: a host matrix is factored on a device copy, which exceeds the budget");
-      return OOC_ERR_BUDGET;
-    }
+    if (bytes > budget)  // out of core: left-looking panels streamed through the budget
+      return spotrf_host_ooc(h, A, n, lda, nb, budget, info, stats);
     if (cudaMalloc(&F.Lf, bytes) != cudaSuccess) { cudaGetLastError(); F.Lf = nullptr; return OOC_ERR_NOMEM; }
     F.ld = n;
     OOC_CUDA_TRY(cudaMemcpy2DAsync(F.Lf, n * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,

@@ -729,3 +729,26 @@ extern "C" void ooc_pdpotrf_(const char* uplo, const int* n, double* a, const in
   int rc = ooc_dpotrf_L(h, A, *n, lld, nbk, budget, &lapack_info, nullptr);
   *info = rc ? rc : lapack_info;
 }
+
+// The same for FP32 (pspotrf_ argument order): ooc_spotrf_L on the sub-matrix.
+extern "C" void ooc_pspotrf_(const char* uplo, const int* n, float* a, const int* ia, const int* ja,
+                             const int* desca, int* info) {
+  if (!info) return;
+  if (!uplo || (*uplo != 'L' && *uplo != 'l')) { *info = -1; return; }
+  if (!n || *n < 0) { *info = -2; return; }
+  if (!ia || !ja || *ia < 1 || *ja < 1) { *info = -4; return; }
+  if (!desca) { *info = -(600 + 1); return; }
+  const int nbk = desca[5], lld = desca[8];
+  if (desca[4] != desca[5]) { *info = -(600 + 5); return; }
+  if (nbk <= 0) { *info = -(600 + 6); return; }
+  if (lld < std::max(1, desca[2])) { *info = -(600 + 9); return; }
+  if (*ia - 1 + *n > desca[2] || *ja - 1 + *n > desca[3]) { *info = -2; return; }
+  ooc_handle* h = ooc_default_handle();
+  if (!h) { *info = OOC_ERR_NODEVICE; return; }
+  size_t budget = 0;
+  if (const char* e = getenv("OOC_DEVICE_BUDGET_MB")) budget = (size_t)atoll(e) << 20;
+  float* A = a + (i64)(*ia - 1) + (i64)(*ja - 1) * lld;
+  int lapack_info = 0;
+  int rc = ooc_spotrf_L(h, A, *n, lld, nbk, budget, &lapack_info, nullptr);
+  *info = rc ? rc : lapack_info;
+}
