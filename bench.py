@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--form", default="mixed", choices=["mixed", "fp64-ooc"])
+    p.add_argument("--form", default="mixed", choices=["mixed", "fp64-ooc", "fp64-ooc-host"])
     p.add_argument("--n", type=int, default=None)
     p.add_argument("--nb", type=int, default=None)
     p.add_argument("--prec", default="bf16x3", choices=["bf16x3", "fp32"])
@@ -63,7 +63,9 @@ def parse():
     p.add_argument("--nrhs", type=int, default=1)
     p.add_argument("--budget-mb", type=int, default=1024, help="device panel budget for the fp64-ooc host leg")
     p.add_argument("--seed", type=int, default=100)
-    p.add_argument("--cpu-sample-n", type=int, default=12288)
+    p.add_argument("--cpu-sample-n", type=int, default=16384)
+    p.add_argument("--cpu-full-n", type=int, default=0,
+                   help="also time the CPU baseline once at this order (the full workload: minutes)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-ref", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
@@ -74,9 +76,9 @@ def parse():
                    help="order of the per-delta forward-error table (each against a plain FP64 solve)")
     a = p.parse_args()
     if a.n is None:
-        a.n = 65536 if a.form == "mixed" else 24576
+        a.n = {"mixed": 65536, "fp64-ooc": 24576, "fp64-ooc-host": 120000}[a.form]
     if a.nb is None:
-        a.nb = 512 if a.form == "mixed" else 1024
+        a.nb = {"mixed": 512, "fp64-ooc": 1024, "fp64-ooc-host": 2500}[a.form]
     return a
 
 
@@ -413,6 +415,68 @@ def run_fp64_ooc(args):
     return 0
 
 
+def run_fp64_ooc_host(args):
+    """The plain FP64 out-of-core factorization of one page-locked host matrix only (no
+    device-resident leg, no second host copy), for orders whose matrix takes most of the
+    host's memory: the reference's own configuration is n=120000, nb=2500 with a 5120 MiB
+    device budget (job.sh:4).  The matrix is regenerated before each step, untimed; the
+    step is ooc_dpotrf_L, timed with CUDA events on the library's compute stream."""
+    import torch
+
+    import oocdag_gb300 as ooc
+
+    ooc.load()
+    n, nb = args.n, args.nb
+    budget = args.budget_mb << 20
+    h = ooc.Handle(0)
+    comp = torch.cuda.ExternalStream(h.stream(0))
+    peak_tf = h.fp64_peak(300.0)
+    link = link_probe()
+    Hw = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    h.set_option(ooc.OPT_PROFILE, 1)
+    steps = []
+    clocks = ClockSampler(0)
+    for r in range(args.warmup + args.steps):
+        h.matgen_uniform(Hw, n, n, args.seed, float(n))
+        torch.cuda.synchronize()
+        if r == args.warmup:
+            clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(comp)
+        res = h.dpotrf_L(Hw, n, n, nb, budget)
+        e1.record(comp)
+        torch.cuda.synchronize()
+        if res.info != 0:
+            raise RuntimeError(f"info={res.info}")
+        if r >= args.warmup:
+            steps.append((e0.elapsed_time(e1), res.stats))
+    clk = clocks.stop()
+    ms = sum(t for t, _ in steps) / len(steps)
+    st = steps[-1][1]
+    value = n ** 3 / 3.0 / (ms / 1e3) / 1e12
+    upd = st["update_flops"] / (st["update_ms"] / 1e3) / 1e12 if st["update_ms"] else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic: A=(R+R^T)/2+n*I, R~U[-0.5,0.5) SplitMix64 seed {args.seed}, regenerated each step",
+        "config": {"workload": f"plain FP64 out-of-core lower Cholesky of a page-locked host matrix n={n} nb={nb}, "
+                               f"device budget {args.budget_mb} MiB (the reference's job.sh:4 configuration)",
+                   "form": "fp64-ooc-host", "n": n, "nb": nb, "budget_mb": args.budget_mb},
+        "panels": st["npanels"], "h2d_bytes": st["h2d_bytes"], "d2h_bytes": st["d2h_bytes"],
+        "host_link_gbs_achieved": (st["h2d_bytes"] + st["d2h_bytes"]) / (ms / 1e3) / 1e9, "host_link_probe": link,
+        "roofline": {"bound": "fp64-dmma", "kernel": "k_panel_update (syrk+gemm, FP64 mma.sync m8n8k4)",
+                     "achieved": upd, "peak": peak_tf, "unit": "TFLOP/s", "frac": upd / peak_tf if upd else None,
+                     "step_frac": value / peak_tf, "launches": st["update_launches"],
+                     "share_of_step": st["update_ms"] / ms if ms else None,
+                     "peak_source": "measured live: FP64 DMMA issue loop on all SMs (ooc_fp64_peak_probe)"},
+        "clocks": clk, "gpu_launches": st["kernel_launches"],
+    }
+    print(json.dumps(line), flush=True)
+    h.close()
+    return 0
+
+
 def _init_dist():
     rank, world, local = dist_env()
     import torch
@@ -728,6 +792,16 @@ def run_mixed(args):
         cpu = {"value": ns_ ** 3 / 3 / tc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"n={ns_} nb={nb}: FP64 factor (the reference's QUARK task graph restated in C++) + "
                          f"dpotrs, {tc:.1f}s on {os.cpu_count()} host threads"}
+        if args.cpu_full_n:  # the same at full size, once: does the sample's rate hold?
+            nf = args.cpu_full_n
+            Af = oracle.gen_uniform(nf, seed, 0.5774 * nf ** 0.5 * (1 + args.delta))
+            bf = np.random.default_rng(1).standard_normal((nf, nrhs))
+            c0 = time.perf_counter()
+            _, info, _ = oracle.cholesky(Af, nb, 1 << 40, os.cpu_count() or 1, 2)
+            oracle.potrs(Af, bf)
+            tf = time.perf_counter() - c0
+            del Af
+            cpu["full_size"] = {"n": nf, "seconds": tf, "value": nf ** 3 / 3 / tf / 1e12, "info": info}
 
     extra = {}
     if rank == 0 and world == 1 and not args.no_extra:
@@ -1111,6 +1185,8 @@ def main():
         return run_reference(args)
     if args.form == "mixed":
         return run_mixed(args)
+    if args.form == "fp64-ooc-host":
+        return run_fp64_ooc_host(args)
     return run_fp64_ooc(args)
 
 

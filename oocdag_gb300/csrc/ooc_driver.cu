@@ -401,40 +401,50 @@ int copy_d2h(Run& R, double* dst, i64 lda, const double* src, i64 ldt, i64 rows,
 // In-panel factorization (oocquark.cpp:389-419).  P maps the panel's tiles; YM / YN are
 // its element extents; col0 its first global column; hostA (may be null) the host
 // address of the panel's tile (0,0) with leading dimension lda.
+// Look-ahead, as QUARK's DAG allows it: the diagonal factor and column solve of tile
+// column j+1 run on the high-priority stream s1 (the handle's host-to-device stream,
+// idle while a panel is factored) beside the bulk of column j's trailing update on
+// s_comp, which first updates tile column j+1 alone and signals s1.  Every tile still
+// receives the same updates, from the same kernels, in the same order.
 int factor_panel(Run& R, const TileMap& P, int Ym, int Yn, i64 YM, i64 YN, i64 col0, double* hostA, i64 lda) {
   ooc_handle* h = R.h;
   const int nb = P.nb;
   const i64 tstride = P.packed ? (i64)nb * nb : (i64)nb;
+  cudaStream_t s0 = h->s_comp, s1 = h->s_h2d;
+  cudaEvent_t evA, evP;  // A: column j+1 updated by column j (s0 -> s1); P: column j solved (s1 -> s0)
+  OOC_CUDA_TRY(next_event(h, &evA));
+  OOC_CUDA_TRY(cudaEventRecord(evA, s0));  // the panel's tiles are ready on s0
   for (int j = 0; j < Yn; j++) {
     const int LN = (int)std::min<i64>(nb, YN - (i64)j * nb);
     double* Djj = tile_ptr(P, j, j);
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s1, evA, 0));
     cudaEvent_t f0 = nullptr, f1 = nullptr;
     if (h->profile) {
       if (next_prof_event(h, &f0) != cudaSuccess || next_prof_event(h, &f1) != cudaSuccess) return OOC_ERR_CUDA;
-      OOC_CUDA_TRY(cudaEventRecord(f0, h->s_comp));
+      OOC_CUDA_TRY(cudaEventRecord(f0, s1));
     }
-    int rc = launch_potrf_tile(Djj, P.ld, LN, col0 + (i64)j * nb, h->d_status, h->s_comp);
+    int rc = launch_potrf_tile(Djj, P.ld, LN, col0 + (i64)j * nb, h->d_status, s1);
     if (rc) return rc;
     R.st.kernel_launches += 3 * ((LN + 63) / 64);
     const int below = Ym - j - 1;
     if (below > 0) {
       const int m_last = (int)(YM - (i64)(Ym - 1) * nb);
       TileCol B{tile_ptr(P, j + 1, j), P.ld, tstride};
-      rc = launch_trsm_col(Djj, P.ld, B, below, nb, m_last, LN, h->d_status, h->s_comp);
+      rc = launch_trsm_col(Djj, P.ld, B, below, nb, m_last, LN, h->d_status, s1);
       if (rc) return rc;
       R.st.kernel_launches += 2 * ((LN + 63) / 64);
     }
     if (h->profile) {
-      OOC_CUDA_TRY(cudaEventRecord(f1, h->s_comp));
+      OOC_CUDA_TRY(cudaEventRecord(f1, s1));
       R.fac_ev.push_back({f0, f1});
     }
+    OOC_CUDA_TRY(next_event(h, &evP));
+    OOC_CUDA_TRY(cudaEventRecord(evP, s1));
+    OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evP, 0));
     if (hostA) {
       // Column j is final: copy it back while the trailing update proceeds
       // (oocquark.cpp:394,409).
-      cudaEvent_t ev;
-      OOC_CUDA_TRY(next_event(h, &ev));
-      OOC_CUDA_TRY(cudaEventRecord(ev, h->s_comp));
-      OOC_CUDA_TRY(cudaStreamWaitEvent(h->s_d2h, ev, 0));
+      OOC_CUDA_TRY(cudaStreamWaitEvent(h->s_d2h, evP, 0));
       for (int i = j; i < Ym; i++) {
         const i64 LM = std::min<i64>(nb, YM - (i64)i * nb);
         rc = copy_d2h(R, hostA + (i64)i * nb + (i64)j * nb * lda, lda, tile_ptr(P, i, j), P.ld, LM, LN, h->s_d2h);
@@ -442,12 +452,23 @@ int factor_panel(Run& R, const TileMap& P, int Ym, int Yn, i64 YM, i64 YN, i64 c
       }
     }
     if (j + 1 < Yn) {
+      // tile column j+1 first, then the rest of the panel's trailing tiles
       TileCol X{tile_ptr(P, j + 1, j), P.ld, tstride};
       TileMap C = P;
       C.base = tile_ptr(P, j + 1, j + 1);
       if (P.packed) C.Ym = Ym - j - 1;
-      rc = timed_update(R, X, C, Ym - j - 1, Yn - j - 1, YM - (i64)(j + 1) * nb, YN - (i64)(j + 1) * nb, nb);
+      rc = timed_update(R, X, C, Ym - j - 1, 1, YM - (i64)(j + 1) * nb, std::min<i64>(nb, YN - (i64)(j + 1) * nb), nb);
       if (rc) return rc;
+      OOC_CUDA_TRY(next_event(h, &evA));
+      OOC_CUDA_TRY(cudaEventRecord(evA, s0));
+      if (j + 2 < Yn) {
+        TileCol X2{tile_ptr(P, j + 2, j), P.ld, tstride};
+        TileMap C2 = P;
+        C2.base = tile_ptr(P, j + 2, j + 2);
+        if (P.packed) C2.Ym = Ym - j - 2;
+        rc = timed_update(R, X2, C2, Ym - j - 2, Yn - j - 2, YM - (i64)(j + 2) * nb, YN - (i64)(j + 2) * nb, nb);
+        if (rc) return rc;
+      }
     }
   }
   return OOC_OK;

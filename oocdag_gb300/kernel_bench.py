@@ -1,12 +1,14 @@
 """Kernel-level micro-benchmarks (CUDA-event timing on the library's compute stream).
 
     python -m oocdag_gb300.kernel_bench syrk  --m 8192 --k 512 --prec bf16x3 [--reps 3]
-    python -m oocdag_gb300.kernel_bench mixed --n 16384 --nb 256 --prec bf16x3
+    python -m oocdag_gb300.kernel_bench mixed --n 16384 --nb 256 --prec bf16x3 [--stored]
     python -m oocdag_gb300.kernel_bench batched --count 2000 --prec fp32 [--reps 2]
 
 ``syrk`` times one trailing-update launch C -= X X^T (lower, FP64 C) in the given
 precision and prints the useful FP64-equivalent rate and the C read+write bandwidth;
-``mixed`` times one mixed-precision factorization plus refinement of a seeded system;
+``mixed`` times one mixed-precision factorization plus refinement of a seeded system
+(generated in place, or with ``--stored`` a stored device matrix, which the library
+factors over left-looking column blocks);
 ``batched`` times the persistent batched factor + solve of `count` seeded small systems.
 These are the commands the profile summaries under profiles/ were captured with.
 """
@@ -61,10 +63,20 @@ def mixed(args) -> None:
     B = torch.empty((1, n), dtype=torch.float64, device="cuda")
     X = torch.empty_like(B)
     h.gen_normal(B, n, n, 1, 7)
+    A = None
+    if args.stored:  # a stored device matrix: the library's left-looking block schedule applies
+        if args.block_cols is not None:
+            h.set_option(ooc.OPT_BLOCK_COLS, args.block_cols)
+        A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        h.matgen_uniform(A, n, n, 100, alpha)
     for prec in args.prec:
         for rep in range(args.reps):
-            F = h.factor_gen(n, 100, alpha, nb, prec)
-            it, be = F.refine_gen(B, n, X, n, 1, 1e-14, 30)
+            if A is not None:
+                F = h.factor(A, n, n, nb, prec)
+                it, be = F.refine(A, n, B, n, X, n, 1, 1e-14, 30)
+            else:
+                F = h.factor_gen(n, 100, alpha, nb, prec)
+                it, be = F.refine_gen(B, n, X, n, 1, 1e-14, 30)
             print(json.dumps({"kind": "mixed", "prec": prec, "n": n, "nb": nb, "rep": rep,
                               "factor_s": F.stats["seconds"], "tflops": n ** 3 / 3 / F.stats["seconds"] / 1e12,
                               "iterations": it, "backward_error": be}), flush=True)
@@ -111,6 +123,9 @@ def main() -> None:
     b.add_argument("--reps", type=int, default=1)
     b.add_argument("--tail-order", type=int, default=None,
                    help="OOC_OPT_TAIL_ORDER for the factor (default: the library's; 0: uniform nb-wide panels)")
+    b.add_argument("--stored", action="store_true",
+                   help="factor a stored device matrix (left-looking blocks) instead of generating it in place")
+    b.add_argument("--block-cols", type=int, default=None, help="OOC_OPT_BLOCK_COLS with --stored")
     c = sub.add_parser("batched")
     c.add_argument("--count", type=int, default=2000)
     c.add_argument("--prec", default="fp32", choices=["fp64", "fp32"])

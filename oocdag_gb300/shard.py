@@ -1,10 +1,12 @@
 """Several GPUs on one matrix: the layout and exchange schedule of the tiled factorization.
 
-Every pool this library runs on has one GPU per box, so the multi-GPU factorization is
-carried here as a host-side schedule that CPU ranks execute (torch.distributed, gloo), with
-the tile arithmetic of the reference's task bodies: dpotrf on the diagonal tile
-(oocquark.cpp:87), dtrsm R/L/T/N below it (:130), dsyrk/dgemm updates of later columns
-(:176, :222).
+The target machine has several GPUs per node, but every call that runs this library's GPU
+code here gets exactly one GPU, so the multi-GPU factorization is carried as a host-side
+schedule that CPU ranks execute (torch.distributed, gloo), with the tile arithmetic of the
+reference's task bodies: dpotrf on the diagonal tile (oocquark.cpp:87), dtrsm R/L/T/N below
+it (:130), dsyrk/dgemm updates of later columns (:176, :222).  It is the schedule a GPU
+rank would follow with the library's kernels in place of those bodies; that GPU path is not
+built, since nothing here could run or measure it.
 
 Layout: tile columns are dealt block-cyclically, column k to rank k % world; a rank keeps
 the full height (rows k*nb .. n-1) of each column it owns, as a GPU would keep them in its
