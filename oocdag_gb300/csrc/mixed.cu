@@ -2254,6 +2254,29 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
     }
     return OOC_OK;
   };
+  // panels q0..q1 into the FP32 matrix: one conversion over their columns (a device
+  // matrix, or the kept copy once its last chunk has arrived), or chunk by chunk through
+  // the staging slots
+  auto convert_panels = [&](int q0, int q1) -> int {
+    if (q1 < q0) return OOC_OK;
+    if (src.on_device || src.keep) {
+      const int k1 = panel_chunks[q1].second - 1;
+      const i64 c0 = col_of(q0), c1 = col_of(q1 + 1);
+      const double* from = src.on_device ? src.A + c0 * src.lda : src.keep + c0 * n;
+      if (!src.on_device) OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evCopied[k1], 0));  // copies land in order
+      k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(c1 - c0, 1024)), 256, 0, s0>>>(
+          from, src.on_device ? src.lda : n, A + c0 * lda, lda, n, c0, (int)(c1 - c0), 0);
+      OOC_CUDA_TRY(cudaGetLastError());
+      next_conv = k1 + 1;
+      if (launches) *launches += 1;
+      return OOC_OK;
+    }
+    for (int q = q0; q <= q1; q++) {
+      int r = convert_panel(q);
+      if (r) return r;
+    }
+    return OOC_OK;
+  };
   // C = trailing matrix from column `c` (rows c..n-1), columns [c, c + w), minus the
   // contribution of the finished panels in columns [0, K): long-K updates from the store
   auto catch_up = [&](i64 c, i64 w, i64 K) -> int {
@@ -2282,7 +2305,7 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
     return launch_split_bf16_f32(A + J0 + LN + J0 * lda, lda, (int)m, LN, F->work2.p, F->work2.bytes, s0);
   };
   if ((rc = enqueue_copies())) return rc;
-  if ((rc = convert_panel(0))) return rc;  // F_0
+  if ((rc = convert_panels(0, 0))) return rc;  // F_0
   OOC_CUDA_TRY(cudaEventRecord(evA, s0));
   {
     i64 J0;
@@ -2297,8 +2320,7 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
     const i64 cn = col_of(plast + 1);         // end of the columns the block's updates reach
     // F_b is final: s1 may factor its diagonal tile (after evA) while s0 converts the rest
     // of the block and F_{b+1} and catches them up with every panel before the block.
-    for (int q = p0 + 1; q <= plast; q++)
-      if ((rc = convert_panel(q))) return rc;
+    if ((rc = convert_panels(p0 + 1, plast))) return rc;
     if ((rc = catch_up(c1, cn - c1, c0))) return rc;  // F_{b+1}
     if ((rc = catch_up(cf, c1 - cf, c0))) return rc;  // the rest of block b
     for (int j = p0; j < p1; j++) {

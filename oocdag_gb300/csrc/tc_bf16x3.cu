@@ -778,6 +778,274 @@ __global__ void __launch_bounds__(THREADS2, 1)
 }
 
 // ---------------------------------------------------------------------------------
+// The same update for long K (the left-looking factor's catch-ups), issued transposed: per
+// K step and product ONE M=128, N=256 MMA with the 128-row B tile as the M operand and the
+// 256-row A tile as the N operand, so TMEM holds the block transposed (lane = C column,
+// TMEM column = C row) and each MMA reads 12 KB of operands from shared memory for 128 x
+// 256 outputs where two M=N=128 MMAs read 16 KB (the MMA stream measured 1.39x faster in
+// isolation).  Same producer, rings, block tickets, bounded waits and teardown as
+// k_syrk2_bf16x3; halves of a block that lie above the diagonal are computed and masked.
+// Epilogue: warp (quad q, group g) reads TMEM lanes 32q.. (32 C columns) and TMEM columns
+// 128g.. (128 C rows) in four 32-row pieces; a thread owns one C column, so a piece is a
+// 32 x 32 box stored column by column with the 128-byte swizzle (conflict-free 16-byte
+// stores) and added into C by one TMA reduction.  Its per-block cost is higher than the
+// K=512 kernel's, which is why only launches with a long K use it.
+// ---------------------------------------------------------------------------------
+constexpr uint32_t IDESC_N256 =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(TB >> 4) << 24);
+__device__ __forceinline__ void umma_bf16_n256(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(IDESC_N256), "r"(accumulate));
+}
+constexpr int TBOX = 32;  // 32 x 32 FP32 C boxes (4 KB, 1024-byte aligned for the swizzle)
+constexpr int BOX2T_OFF = STAGES2 * STAGE2_BYTES + 1024;  // after the control block, padded
+constexpr int SMEM2T_BYTES = BOX2T_OFF + EPI2_WARPS * TBOX * TBOX * 4 + 1024 /*align*/;  // 231,424
+static_assert(SMEM2T_BYTES <= 232448, "transposed update kernel shared memory");
+
+__global__ void __launch_bounds__(THREADS2, 1)
+    k_syrk2t_bf16x3(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
+                    const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
+                    const __grid_constant__ CUtensorMap map_c, int m, int Kp, int T, int bj_lo, int bj_hi, i64 nblk,
+                    unsigned long long* __restrict__ tickets, int* status) {
+  if (*(volatile int*)status) return;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
+  uint64_t* empty = full + STAGES2;
+  uint64_t* tfull = empty + STAGES2;
+  uint64_t* tempty = tfull + NSLOT2;
+  uint64_t* done = tempty + NSLOT2;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  volatile long long* n_issued = (volatile long long*)(smem + STAGES2 * STAGE2_BYTES + 128);
+  volatile long long* n_consumed = n_issued + 1;
+  uint64_t* idfull = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + 160);
+  uint64_t* idempty = idfull + NID2;
+  volatile long long* ids = (volatile long long*)(idempty + NID2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = Kp / TK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES2; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < NSLOT2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], EPI2_WARPS);
+    }
+    for (int a = 0; a < NID2; a++) {
+      mbar_init(&idfull[a], 1);
+      mbar_init(&idempty[a], 1 + EPI2_WARPS);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    *n_issued = 0;
+    *n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS2));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---- TMA producer: as in k_syrk2_bf16x3
+    long long c = 0;
+    bool ok = true;
+    i64 t = blockIdx.x;
+    for (int tl = 0; ok; tl++) {
+      const i64 tp = t < nblk ? t : -1;
+      if (lane == 0) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idempty[r], (uint32_t)(((tl / NID2) & 1) ^ 1), abort_flag)) {
+          ok = false;
+        } else {
+          ids[r] = tp;
+          mbar_arrive(&idfull[r]);
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok || tp < 0) break;
+      int bi2, bj;
+      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+      const bool b_in_a = (bj == 2 * bi2 || bj == 2 * bi2 + 1);
+      for (int kc = 0; kc < nk; kc++, c++) {
+        if (lane == 0) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
+            ok = false;
+          } else {
+            uint8_t* st = smem + s * STAGE2_BYTES;
+            mbar_expect_tx(&full[s], b_in_a ? 2 * A2_PLANE : STAGE2_BYTES);
+            tma_load_2d(st, &map_ahi, &full[s], kc * TK, bi2 * TM2);
+            tma_load_2d(st + A2_PLANE, &map_alo, &full[s], kc * TK, bi2 * TM2);
+            if (!b_in_a) {
+              tma_load_2d(st + 2 * A2_PLANE, &map_bhi, &full[s], kc * TK, bj * TB);
+              tma_load_2d(st + 2 * A2_PLANE + B2_PLANE, &map_blo, &full[s], kc * TK, bj * TB);
+            }
+            *n_issued = c + 1;
+          }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+      }
+      if (!ok) break;
+      unsigned long long nx = 0;
+      if (lane == 0) nx = atomicAdd(tickets, 1ull);
+      nx = __shfl_sync(0xffffffffu, nx, 0);
+      t = (i64)gridDim.x + (i64)nx;
+    }
+    if (!ok && lane == 0) *abort_flag = 1;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: per stage and K-step, the three products as N=256 MMAs (D transposed)
+      long long c = 0;
+      bool ok = true;
+      for (int tl = 0;; tl++) {
+        const int r = tl % NID2;
+        if (!mbar_wait(&idfull[r], (uint32_t)((tl / NID2) & 1), abort_flag)) { ok = false; break; }
+        const i64 t = ids[r];
+        mbar_arrive(&idempty[r]);
+        if (t < 0) break;
+        int bi2, bj;
+        strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+        const int slot = tl % NSLOT2;
+        if (!mbar_wait(&tempty[slot], (uint32_t)(((tl / NSLOT2) & 1) ^ 1), abort_flag)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        const uint32_t d = tmem + (uint32_t)(slot * 2 * TB);
+        for (int kc = 0; kc < nk; kc++, c++) {
+          const int s = (int)(c % STAGES2);
+          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
+          *n_consumed = c + 1;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+          const uint32_t base = smem_u32(smem + s * STAGE2_BYTES);
+          const uint32_t a_hi = base, a_lo = base + A2_PLANE;
+          const uint32_t half_b = (uint32_t)(TB * 128);
+          uint32_t b_hi = base + 2 * A2_PLANE, b_lo = base + 2 * A2_PLANE + B2_PLANE;
+          if (bj == 2 * bi2) { b_hi = a_hi; b_lo = a_lo; }
+          if (bj == 2 * bi2 + 1) { b_hi = a_hi + half_b; b_lo = a_lo + half_b; }
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; kk++) {
+            const uint32_t off = kk * 32;
+            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+            umma_bf16_n256(d, umma_desc_sw128(b_hi + off), umma_desc_sw128(a_hi + off), acc0);
+            umma_bf16_n256(d, umma_desc_sw128(b_hi + off), umma_desc_sw128(a_lo + off), 1u);
+            umma_bf16_n256(d, umma_desc_sw128(b_lo + off), umma_desc_sw128(a_hi + off), 1u);
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[slot]);
+      }
+      if (!ok) *abort_flag = 1;
+    }
+  } else {
+    // ---- epilogue: warp (quad q, group g): C columns bj*128 + 32q + lane, C rows
+    // bi2*256 + 128g + 32 piece + (0..31); one 32 x 32 box per piece, 128-byte swizzled.
+    const int quad = warp & 3;
+    const int grp = (warp - 2) >> 2;
+    float* box = reinterpret_cast<float*>(smem + BOX2T_OFF) + (warp - 2) * TBOX * TBOX;
+    auto next_id = [&](int u) -> i64 {
+      const int r = u % NID2;
+      const bool got = mbar_wait(&idfull[r], (uint32_t)((u / NID2) & 1), abort_flag);
+      i64 v = -2;
+      if (__all_sync(0xffffffffu, got)) v = ids[r];
+      __syncwarp();
+      if (lane == 0 && v != -2) mbar_arrive(&idempty[r]);
+      return v;
+    };
+    i64 t = next_id(0);
+    for (int tl = 0; t >= 0; tl++) {
+      int bi2, bj;
+      strip2_decode(t, T, bj_lo, bj_hi, &bi2, &bj);
+      const int slot = tl % NSLOT2;
+      const bool got = mbar_wait(&tfull[slot], (uint32_t)((tl / NSLOT2) & 1), abort_flag);
+      if (!__all_sync(0xffffffffu, got)) {
+        t = -2;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+      const int col = bj * TB + quad * 32 + lane;  // this thread's C column
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(slot * 2 * TB + grp * 128);
+#pragma unroll 1
+      for (int piece = 0; piece < 4; piece++) {
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr + (uint32_t)(32 * piece)));
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr + (uint32_t)(32 * piece + 16)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::);
+        const int row0 = bi2 * TM2 + grp * 128 + piece * 32;
+        if (lane == 0) bulk_wait_read<0>();  // the previous piece's reduction has read the box
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 8; j++) {  // 16-byte chunk j: rows row0 + 4j .. +3
+          float4 q4;
+          float* f = reinterpret_cast<float*>(&q4);
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const int row = row0 + 4 * j + e;
+            f[e] = (col <= row) ? -__uint_as_float(v[4 * j + e]) : -0.0f;
+          }
+          *reinterpret_cast<float4*>(box + lane * TBOX + ((j ^ (lane & 7)) * 4)) = q4;
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          tma_reduce_add_2d(&map_c, box, row0, bj * TB + quad * 32);
+          bulk_commit();
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[slot]);
+      t = next_id(tl + 1);
+    }
+    if (lane == 0) bulk_wait_all();
+    if (t == -2 && lane == 0) *abort_flag = 1;
+  }
+
+  // ---- teardown (as in k_syrk2_bf16x3)
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  if (*abort_flag) {
+    if (threadIdx.x == 0) atomicCAS(status, 0, ERR_TIMEOUT_CODE);
+    if (warp == 1 && lane == 0) {
+      umma_commit(done);
+      (void)mbar_wait(done, 0, nullptr);
+    }
+    if (warp == 0 && lane == 0) {
+      for (long long c = *n_consumed; c < *n_issued; c++)
+        (void)mbar_wait(&full[c % STAGES2], (uint32_t)((c / STAGES2) & 1), nullptr);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS2));
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // Column solve of a panel on the tensor cores: P = U X^T (m x nb), U the panel before the
 // solve and X = L_jj^{-1} (lower triangular), both given as BF16 hi/lo planes (K-major),
 // with the update's three products.  Block t = (row tile bi2 of 256 rows, column block cb
@@ -1067,6 +1335,19 @@ int make_map_c32(CUtensorMap* map, float* C, int m, i64 ldc) {
   return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
 }
 
+// FP32 C for the transposed update's reductions: 32 x 32 boxes (rows innermost), 128-byte
+// swizzle (the epilogue stores each box column by column with the same swizzle).
+int make_map_c32t(CUtensorMap* map, float* C, int m, i64 ldc) {
+  cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)m};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)TBOX, (cuuint32_t)TBOX};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
+}
+
 // Number of 256 x 128 blocks of k_syrk2_bf16x3 for block columns [bj_lo, bj_hi).
 i64 count_blocks2(int T, int bj_lo, int bj_hi) {
   const int T2 = (T + 1) / 2;
@@ -1241,9 +1522,14 @@ int launch_trsm_bf16x3_f32(void* uwork, size_t ubytes, const void* xhi, const vo
 // row r's K values at hi + r * ldk, lo + r * ldk (for example a window of a matrix-wide
 // plane store: rows from the trailing matrix's first row, K over any run of finished
 // panels).  `tickets` is 8 bytes of device memory for the launch's block counter.
+int g_long_k = 2048;  // K from which the transposed kernel is used (OOC_SYRK_LONG_K overrides)
 int launch_syrk_planes_f32(const void* hi, const void* lo, i64 ldk, int m, int K, float* C, i64 ldc,
                            const int* status, cudaStream_t s, unsigned long long* tickets, int bj_lo, int bj_hi,
                            int reserve_sms) {
+  static const int kLongK = [] {
+    const char* e = getenv("OOC_SYRK_LONG_K");
+    return e ? atoi(e) : g_long_k;
+  }();
   if (m <= 0 || K <= 0) return OOC_OK;
   if (!status || !hi || !lo || !tickets || K % TK != 0 || ldk < K) return OOC_ERR_INTERNAL;
   if ((reinterpret_cast<uintptr_t>(hi) | reinterpret_cast<uintptr_t>(lo) | (uintptr_t)(ldk * 2)) % 16 != 0)
@@ -1264,20 +1550,29 @@ int launch_syrk_planes_f32(const void* hi, const void* lo, i64 ldk, int m, int K
     return OOC_ERR_CUDA;
   }
   if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && (ldc * (i64)sizeof(float)) % 16 == 0) {
+    // long K (catch-ups): the transposed N=256 kernel; short K: the K=512-tuned one
+    const bool tr = K >= kLongK;
     CUtensorMap ah, al, mc;
-    if (make_map(&ah, h, m, K, TM2, ldk) || make_map(&al, l, m, K, TM2, ldk) || make_map_c32(&mc, C, m, ldc)) {
+    if (make_map(&ah, h, m, K, TM2, ldk) || make_map(&al, l, m, K, TM2, ldk) ||
+        (tr ? make_map_c32t(&mc, C, m, ldc) : make_map_c32(&mc, C, m, ldc))) {
       ooc_set_last_message("cuTensorMapEncodeTiled failed for the update operands");
       return OOC_ERR_CUDA;
     }
     const i64 nblk2 = count_blocks2((int)T, bj_lo, bj_hi);
     if (nblk2 <= 0) return OOC_OK;
-    OOC_CUDA_TRY(
-        cudaFuncSetAttribute(k_syrk2_bf16x3<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2U_BYTES));
     const i64 grid2 = std::max<i64>(1, std::min<i64>(nblk2, std::max(1, nsm - std::max(0, reserve_sms))));
     OOC_CUDA_TRY(cudaMemsetAsync(tickets, 0, sizeof(unsigned long long), s));
-    k_syrk2_bf16x3<float><<<(unsigned)grid2, THREADS2, SMEM2U_BYTES, s>>>(ah, al, mh, ml, mc, m, K, (int)T, bj_lo,
-                                                                          bj_hi, nblk2, tickets,
-                                                                          const_cast<int*>(status));
+    if (tr) {
+      OOC_CUDA_TRY(cudaFuncSetAttribute(k_syrk2t_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2T_BYTES));
+      k_syrk2t_bf16x3<<<(unsigned)grid2, THREADS2, SMEM2T_BYTES, s>>>(ah, al, mh, ml, mc, m, K, (int)T, bj_lo, bj_hi,
+                                                                       nblk2, tickets, const_cast<int*>(status));
+    } else {
+      OOC_CUDA_TRY(
+          cudaFuncSetAttribute(k_syrk2_bf16x3<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM2U_BYTES));
+      k_syrk2_bf16x3<float><<<(unsigned)grid2, THREADS2, SMEM2U_BYTES, s>>>(ah, al, mh, ml, mc, m, K, (int)T, bj_lo,
+                                                                            bj_hi, nblk2, tickets,
+                                                                            const_cast<int*>(status));
+    }
     OOC_CUDA_TRY(cudaGetLastError());
     return OOC_OK;
   }
