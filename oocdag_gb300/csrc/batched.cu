@@ -281,9 +281,11 @@ __device__ void solve_one(const T* __restrict__ L, int n, T* __restrict__ b) {
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(BT) k_batched_posv(const Item* __restrict__ items, int count, int* info,
-                                                     int* counter, int do_solve) {
+// MINB resident CTAs per SM requested from the register allocator: 2 for FP32 (whose
+// shared memory, sized per size class, lets two CTAs share an SM up to n = 256), 1 for FP64.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_batched_posv(const Item* __restrict__ items, int count, int* info,
+                                                           int* counter, int do_solve) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   T* D = (T*)smem_raw;
   T* P = D + 64 * 65;
@@ -317,8 +319,11 @@ __global__ void k_scatter_info(const int* sorted_info, const int* order, int cou
   if (i < count) out[order[i]] = sorted_info[i];
 }
 
+// Shared memory of a launch whose matrices have orders <= nmax and panel widths <= blk.
 template <typename T>
-size_t smem_for(int blk) { return (size_t)(64 * 65 + NMAX * (blk + 1)) * sizeof(T); }
+size_t smem_for(int blk, int nmax = NMAX) { return (size_t)(64 * 65 + nmax * (blk + 1)) * sizeof(T); }
+template <typename T>
+constexpr int minb() { return sizeof(T) == 4 ? 2 : 1; }
 
 template <typename T>
 int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
@@ -336,8 +341,8 @@ int run_batched(ooc_handle* h, int count, const int* n, const int64_t* a_off, co
 }
 
 // Sorts the items by decreasing order, picks each one's panel width from the table, and
-// runs them in one persistent launch on `s`; info_host receives LAPACK info per item in
-// the caller's order.
+// runs them in persistent launches on `s`, one per size class; info_host receives LAPACK
+// info per item in the caller's order.
 template <typename T>
 int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_host, const int* blk_table,
               int ctas_per_sm, int do_solve, double* seconds, int (*wait)(void*, cudaStream_t), void* wait_arg,
@@ -347,7 +352,6 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return items_in[x].n > items_in[y].n; });
   std::vector<Item> items(count);
-  int maxblk = 1;
   for (int i = 0; i < count; i++) {
     const int j = order[i];
     const int bucket = std::min(NBUCKETS - 1, items_in[j].n / 32);
@@ -356,10 +360,26 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
     blk = blk <= 8 ? 8 : blk <= 16 ? 16 : blk <= 32 ? 32 : 64;  // the compiled widths
     items[i] = items_in[j];
     items[i].blk = blk;
-    maxblk = std::max(maxblk, blk);
   }
+  // Size classes (orders in (0,64], (64,128], (128,256], (256,384], (384,512]; the items
+  // are sorted by decreasing order, so a class is a contiguous range): one persistent
+  // launch each, its shared memory sized for the class's largest order and panel width,
+  // so that the small classes fit several CTAs per SM.
+  const int bounds[] = {512, 384, 256, 128, 64};
+  std::vector<std::pair<int, int>> classes;  // [first, one past the last) in sorted order
+  {
+    int i = 0;
+    for (int ci = 0; ci < 5 && i < count; ci++) {
+      const int lo = ci + 1 < 5 ? bounds[ci + 1] : 0;
+      int j = i;
+      while (j < count && items[j].n > lo) j++;
+      if (j > i) classes.emplace_back(i, j);
+      i = j;
+    }
+  }
+  const int ncls = (int)classes.size();
   // the launch tables, in the caller's workspace (kept across calls): items, then four
-  // int arrays (info, order, scattered info, counter), each 256-byte aligned
+  // int arrays (info, order, scattered info, one counter per class), each 256-byte aligned
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t b_items = up(sizeof(Item) * (size_t)count), b_int = up(sizeof(int) * (size_t)count);
   int rc = ws->ensure(b_items + 3 * b_int + 256);
@@ -377,27 +397,36 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
   if (!rc) {
     cudaMemcpyAsync(d_items, items.data(), sizeof(Item) * count, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(d_counter, 0, sizeof(int), s);
-    const size_t sm = smem_for<T>(maxblk);
-    if (cudaFuncSetAttribute(k_batched_posv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
-      cudaGetLastError();
-      rc = OOC_ERR_UNSUPPORTED;
-    } else {
-      int nsm = 0;
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaMemsetAsync(d_counter, 0, sizeof(int) * 8, s);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    for (int ci = 0; ci < ncls && !rc; ci++) {
+      const int i0 = classes[ci].first, i1 = classes[ci].second;
+      int cmax = 1, cblk = 1;
+      for (int i = i0; i < i1; i++) {
+        cmax = std::max(cmax, items[i].n);
+        cblk = std::max(cblk, items[i].blk);
+      }
+      const size_t sm = smem_for<T>(cblk, cmax);
+      if (cudaFuncSetAttribute(k_batched_posv<T, minb<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        rc = OOC_ERR_UNSUPPORTED;
+        break;
+      }
       int occ = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_posv<T>, BT, sm);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_posv<T, minb<T>()>, BT, sm);
       const int per = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : occ, std::max(occ, 1)));
-      const int grid = std::max(1, std::min(count, nsm * per));
-      cudaEventCreate(&e0);
-      cudaEventCreate(&e1);
-      cudaEventRecord(e0, s);
-      k_batched_posv<T><<<grid, BT, sm, s>>>(d_items, count, d_info, d_counter, do_solve);
-      cudaEventRecord(e1, s);
-      k_scatter_info<<<(count + 255) / 256, 256, 0, s>>>(d_info, d_order, count, d_out);
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) { ooc_set_last_error(e, "k_batched_posv", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
+      const int grid = std::max(1, std::min(i1 - i0, nsm * per));
+      k_batched_posv<T, minb<T>()><<<grid, BT, sm, s>>>(d_items + i0, i1 - i0, d_info + i0, d_counter + ci, do_solve);
     }
+    cudaEventRecord(e1, s);
+    if (!rc) k_scatter_info<<<(count + 255) / 256, 256, 0, s>>>(d_info, d_order, count, d_out);
+    cudaError_t e = cudaGetLastError();
+    if (!rc && e != cudaSuccess) { ooc_set_last_error(e, "k_batched_posv", __FILE__, __LINE__); rc = OOC_ERR_CUDA; }
   }
   if (!rc) {
     cudaMemcpyAsync(info_host, d_out, sizeof(int) * count, cudaMemcpyDeviceToHost, s);
