@@ -253,38 +253,82 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
 
 // ---------------------------------------------------------------------------------
 // B := B L^-T for a block of up to 64 columns: L is n x n lower (n <= 64), B rows are
-// independent.  One thread per row, 64 rows per CTA; z = blockIdx.y walks a batch of
-// row panels (tiles) with stride sB, the last of which has m_last rows.
+// independent.  One thread per row, TS_ROWS rows per CTA (small CTAs spread a short
+// panel over more SMs: FP64 issues at ~2 FMAs per clock per SM); z = blockIdx.y walks a
+// batch of row panels (tiles) with stride sB, the last of which has m_last rows.
+// Right-looking inside the row: once x_c is final, every later column takes its FMA with
+// it, so a row's 2016 FMAs are independent across columns instead of one dependent chain
+// per column; each column still receives its updates in increasing q.  The row is done
+// in two halves of 32 columns held in registers; the first half's results wait in shared
+// memory while they update the second.  L sits in shared memory, padded to 64 with the
+// identity, and is read by broadcast; x_c = v * (1 / L(c,c)).
 // ---------------------------------------------------------------------------------
-__global__ void __launch_bounds__(64) k_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB,
-                                                   int m, int m_last, int batch, int n,
-                                                   const int* status) {
+constexpr int TS_ROWS = 32;
+constexpr int TS_H = SB / 2;
+
+// x[0..TS_H) := x L(c0.., c0..)^-T for the 32 columns starting at c0, right-looking.
+// `zero` is 0 at run time; adding (zero & bits of x_c) to the address makes column c's
+// loads of L wait for x_c, so the compiler does not hoist all 496 loads into registers.
+__device__ __forceinline__ void trsm_half(double (&x)[TS_H], const double* Ls, const double* Rinv, int c0,
+                                          int zero) {
+#pragma unroll
+  for (int c = 0; c < TS_H; c++) {
+    x[c] *= Rinv[c0 + c];
+    const double* lc = Ls + (c0 + c) * SB + c0 + (zero & __double2hiint(x[c]));
+#pragma unroll
+    for (int q = c + 1; q < TS_H; q++) x[q] = fma(-x[c], lc[q], x[q]);
+  }
+}
+
+__global__ void __launch_bounds__(TS_ROWS) k_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB,
+                                                        int m, int m_last, int batch, int n,
+                                                        const int* status) {
   if (status && *(volatile const int*)status) return;
-  extern __shared__ double smem[];
-  double* Ls = smem;             // Ls[c * SB + r] = L(r, c)
-  double* Xs = smem + SB * SB;   // Xs[c * 64 + row]
+  __shared__ __align__(16) double Ls[SB * SB];  // Ls[c * SB + r] = L(r, c)
+  __shared__ double Rinv[SB];
+  __shared__ double Xs[TS_H * TS_ROWS];         // first half's results, Xs[c * TS_ROWS + t]
   const int t = threadIdx.x;
   const int z = blockIdx.y;
   const int mz = (z == batch - 1) ? m_last : m;
-  const int r0 = blockIdx.x * 64;
+  const int r0 = blockIdx.x * TS_ROWS;
   if (r0 >= mz) return;
   double* Bz = B + (i64)z * sB;
-  for (int idx = t; idx < n * n; idx += 64) {
-    int c = idx / n, r = idx % n;
-    Ls[c * SB + r] = (r >= c) ? L[r + (i64)c * ldl] : 0.0;
+  for (int idx = t; idx < SB * SB; idx += TS_ROWS) {
+    const int c = idx / SB, r = idx % SB;
+    double v = (r == c) ? 1.0 : 0.0;
+    if (r < n && c < n && r >= c) v = L[r + (i64)c * ldl];
+    Ls[idx] = v;
   }
-  const int row = r0 + t;
-  const bool live = row < mz;
-  for (int c = 0; c < n; c++) Xs[c * 64 + t] = live ? Bz[row + (i64)c * ldb] : 0.0;
   __syncthreads();
-  // x_c = (b_c - sum_{q<c} x_q L(c,q)) / L(c,c)
-  for (int c = 0; c < n; c++) {
-    double v = Xs[c * 64 + t];
-    for (int q = 0; q < c; q++) v = fma(-Xs[q * 64 + t], Ls[q * SB + c], v);
-    Xs[c * 64 + t] = v / Ls[c * SB + c];
+  for (int c = t; c < SB; c += TS_ROWS) Rinv[c] = 1.0 / Ls[c * SB + c];
+  const int row = r0 + t;
+  const int nl = (row < mz) ? n : 0;  // columns this thread loads and stores
+  double* p = Bz + (row < mz ? row : 0);
+  double x[TS_H];
+#pragma unroll
+  for (int c = 0; c < TS_H; c++) x[c] = (c < nl) ? p[(i64)c * ldb] : 0.0;
+  __syncthreads();
+  const int zero = n >> 30;  // n <= 64
+  trsm_half(x, Ls, Rinv, 0, zero);
+#pragma unroll
+  for (int c = 0; c < TS_H; c++) {
+    Xs[c * TS_ROWS + t] = x[c];
+    if (c < nl) p[(i64)c * ldb] = x[c];
   }
-  if (live)
-    for (int c = 0; c < n; c++) Bz[row + (i64)c * ldb] = Xs[c * 64 + t];
+  if (n <= TS_H) return;
+#pragma unroll
+  for (int c = 0; c < TS_H; c++) x[c] = (TS_H + c < nl) ? p[(i64)(TS_H + c) * ldb] : 0.0;
+  // the second half's updates from the first half, in increasing c
+  for (int c = 0; c < TS_H; c++) {
+    const double xc = Xs[c * TS_ROWS + t];
+    const double* lc = Ls + c * SB + TS_H + (zero & __double2hiint(xc));
+#pragma unroll
+    for (int q = 0; q < TS_H; q++) x[q] = fma(-xc, lc[q], x[q]);
+  }
+  trsm_half(x, Ls, Rinv, TS_H, zero);
+#pragma unroll
+  for (int c = 0; c < TS_H; c++)
+    if (TS_H + c < nl) p[(i64)(TS_H + c) * ldb] = x[c];
 }
 
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
@@ -338,15 +382,12 @@ int launch_gemm_nt_trib(const double* A, i64 lda, const double* B, i64 ldb, doub
   return launch_gemm_batched(gb, status, s);
 }
 
-static int trsm_small_smem() { return (SB * SB + SB * 64) * (int)sizeof(double); }
-
 static int launch_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB, int m, int m_last,
                              int batch, int n, const int* status, cudaStream_t s) {
   if (batch <= 0 || n <= 0) return OOC_OK;
-  // per device: set on every launch (cheap)
-  OOC_CUDA_TRY(cudaFuncSetAttribute(k_trsm_small, cudaFuncAttributeMaxDynamicSharedMemorySize, trsm_small_smem()));
-  dim3 grid((max(m, m_last) + 63) / 64, batch);
-  k_trsm_small<<<grid, 64, trsm_small_smem(), s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
+  if (n > SB) return OOC_ERR_INTERNAL;
+  dim3 grid((max(m, m_last) + TS_ROWS - 1) / TS_ROWS, batch);
+  k_trsm_small<<<grid, TS_ROWS, 0, s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }

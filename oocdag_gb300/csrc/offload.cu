@@ -113,21 +113,44 @@ __global__ void k_scale(double* C, i64 ldc, int m, int n, double beta, int mask)
 
 // Lower-form copy of a triangular matrix: L(i,j) = T(i,j) (uplo L) or T(j,i) (uplo U) for
 // i >= j, with a unit diagonal when requested; zero above.
-__global__ void k_lower_form(const double* T, i64 ldt, double* L, i64 ldl, int n, int upper, int unit) {
+// Lower triangle M (order n, zero above the diagonal) read from the triangle T through one
+// of four index maps, so that every dtrsm form becomes the column solve W := W M^-T:
+//   mode 0: M = L          M(i,j) = T(i, j)
+//   mode 1: M = U^T        M(i,j) = T(j, i)
+//   mode 2: M = J L^T J    M(i,j) = T(n-1-j, n-1-i)   (J reverses the order)
+//   mode 3: M = J U J      M(i,j) = T(n-1-i, n-1-j)
+// A unit diagonal is written as ones (T's diagonal is not read).
+__global__ void k_tri_form(const double* T, i64 ldt, double* M, i64 ldm, int n, int mode, int unit) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   for (int j = blockIdx.y; j < n; j += gridDim.y) {
     double v = 0.0;
-    if (i > j) v = upper ? T[j + (i64)i * ldt] : T[i + (i64)j * ldt];
-    else if (i == j) v = unit ? 1.0 : T[i + (i64)i * ldt];
-    L[i + (i64)j * ldl] = v;
+    if (i > j || (i == j && !unit)) {
+      int r = i, c = j;
+      if (mode == 1) { r = j; c = i; }
+      else if (mode == 2) { r = n - 1 - j; c = n - 1 - i; }
+      else if (mode == 3) { r = n - 1 - i; c = n - 1 - j; }
+      v = T[r + (i64)c * ldt];
+    } else if (i == j) {
+      v = 1.0;
+    }
+    M[i + (i64)j * ldm] = v;
   }
 }
 
-__global__ void k_identity(double* D, i64 ld, int n) {
+// W (rows x cols, ld ldw) <-> B: W(i, j) sits at S(i, rev ? cols-1-j : j) with S = B or B^T.
+// TO_W: W = alpha * that element; otherwise the element = W(i, j).
+template <bool TO_W>
+__global__ void k_b_map(double* B, i64 ldb, double* W, i64 ldw, int rows, int cols, int trans, int rev,
+                        double alpha) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int j = blockIdx.y; j < n; j += gridDim.y) D[i + (i64)j * ld] = (i == j) ? 1.0 : 0.0;
+  if (i >= rows) return;
+  for (int j = blockIdx.y; j < cols; j += gridDim.y) {
+    const int jj = rev ? cols - 1 - j : j;
+    double* e = trans ? &B[jj + (i64)i * ldb] : &B[i + (i64)jj * ldb];
+    if (TO_W) W[i + (i64)j * ldw] = alpha * *e;
+    else *e = W[i + (i64)j * ldw];
+  }
 }
 
 // Transposed copy of the upper triangle into / out of lower form.
@@ -394,37 +417,33 @@ extern "C" void offload_dtrsm(const char* side, const char* uplo, const char* tr
     finish(s);
     return;
   }
-  // Other forms: D = L^-T with L the lower form of the triangle, then one contraction.
-  // op(T)^-1 = D for (L,T) and (U,N); D^T for (L,N) and (U,T).
-  double *Lw = nullptr, *D = nullptr, *W = nullptr;
-  if (cudaMalloc(&Lw, (size_t)kdim * kdim * 8) != cudaSuccess || cudaMalloc(&D, (size_t)kdim * kdim * 8) != cudaSuccess ||
-      cudaMalloc(&W, (size_t)(*m) * (*n) * 8) != cudaSuccess) {
+  // Every other form is the same column solve (substitution, no explicit inverse) on
+  // rearranged copies.  Side L transposes first: op(T) X = B  <=>  X^T op(T)^T = B^T.
+  // On side R, X op(T) = B with op(T) = L^T is the direct form (M = L); U = (U^T)^T gives
+  // M = U^T; a lower (or upper-transposed) right factor is reversed into an upper one,
+  // X L J = B J  <=>  (X J)(J L J) = B J, whose transpose-lower form is M = J L^T J
+  // (J U J for X U^T = B), with the columns of B and of the result in reverse order.
+  const bool tr = (sd == 'L');
+  const char te = tr ? (t == 'N' ? 'T' : 'N') : (t == 'N' ? 'N' : 'T');  // the side-R form's op
+  const int mode = (u == 'L') ? (te == 'T' ? 0 : 2) : (te == 'N' ? 1 : 3);
+  const int rev = mode >= 2;
+  const int rows = tr ? *n : *m;  // W = alpha * (B or B^T), rows x kdim, columns maybe reversed
+  double *M = nullptr, *W = nullptr;
+  if (cudaMalloc(&M, (size_t)kdim * kdim * 8) != cudaSuccess || cudaMalloc(&W, (size_t)rows * kdim * 8) != cudaSuccess) {
     cudaGetLastError();
-    if (Lw) cudaFree(Lw);
-    if (D) cudaFree(D);
+    if (M) cudaFree(M);
     t_err = OOC_ERR_NOMEM;
     return;
   }
-  dim3 g2((kdim + 255) / 256, std::min(kdim, 4096));
-  k_lower_form<<<g2, 256, 0, s>>>(a, *lda, Lw, kdim, kdim, u == 'U', d == 'U');
-  k_identity<<<g2, 256, 0, s>>>(D, kdim, kdim);
-  int rc = launch_trsm_col(Lw, kdim, TileCol{D, kdim, 0}, 1, kdim, kdim, kdim, sl->status, s);
+  dim3 gm((kdim + 255) / 256, std::min(kdim, 4096)), gw((rows + 255) / 256, std::min(kdim, 4096));
+  k_tri_form<<<gm, 256, 0, s>>>(a, *lda, M, kdim, kdim, mode, d == 'U');
+  k_b_map<true><<<gw, 256, 0, s>>>(b, *ldb, W, rows, rows, kdim, tr, rev, *alpha);
+  int rc = launch_trsm_col(M, kdim, TileCol{W, rows, 0}, 1, rows, rows, kdim, sl->status, s);
   if (rc) t_err = rc;
-  const bool useD = (u == 'L' && t != 'N') || (u == 'U' && t == 'N');
-  // M = useD ? D : D^T ; M(i,j) = useD ? D[i + j*kdim] : D[j + i*kdim]
-  if (sd == 'L') {
-    // W = alpha M B  (M: m x m, B: m x n) -> opA = M (rows i, k), opB(j,kk) = B[kk + j*ldb]
-    const i64 sar = useD ? 1 : kdim, sak = useD ? kdim : 1;
-    gemm_general(D, sar, sak, b, *ldb, 1, W, *m, *m, *n, *m, *alpha, 0.0, 0, s);
-  } else {
-    // W = alpha B M  (B: m x n, M: n x n) -> opA = B, opB(j,kk) = M(kk, j)
-    const i64 sbr = useD ? kdim : 1, sbk = useD ? 1 : kdim;
-    gemm_general(b, 1, *ldb, D, sbr, sbk, W, *m, *m, *n, *n, *alpha, 0.0, 0, s);
-  }
-  cudaMemcpy2DAsync(b, (size_t)(*ldb) * 8, W, (size_t)(*m) * 8, (size_t)(*m) * 8, *n, cudaMemcpyDeviceToDevice, s);
+  k_b_map<false><<<gw, 256, 0, s>>>(b, *ldb, W, rows, rows, kdim, tr, rev, 1.0);
+  if (cudaGetLastError() != cudaSuccess) t_err = OOC_ERR_CUDA;
   finish(s);
-  cudaFree(Lw);
-  cudaFree(D);
+  cudaFree(M);
   cudaFree(W);
 }
 

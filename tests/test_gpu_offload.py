@@ -132,6 +132,32 @@ def test_dtrsm(off, side, uplo, trans, diag):
     off.Free(pb)
 
 
+@pytest.mark.parametrize("side,uplo,trans,diag", list(itertools.product("LR", "LU", "NT", "NU")))
+def test_dtrsm_ill_conditioned_is_backward_stable(off, side, uplo, trans, diag):
+    # A random triangle of order 200 has a condition number near 1e17: every form must
+    # still leave a residual at FP64 rounding level (substitution, not an explicit inverse:
+    # LAPACK's substitution gives 1e-21..4e-18 on these inputs, an explicit inverse up to 6e-17).
+    rng = np.random.default_rng(17)
+    m, n = 200, 130
+    kd = m if side == "L" else n
+    T = rng.standard_normal((kd, kd))
+    np.fill_diagonal(T, rng.uniform(0.5, 1.5, kd) * np.sign(rng.standard_normal(kd)))
+    B = rng.standard_normal((m, n))
+    alpha = -1.5
+    Tt = np.tril(T) if uplo == "L" else np.triu(T)
+    if diag == "U":
+        np.fill_diagonal(Tt, 1.0)
+    opT = Tt if trans == "N" else Tt.T
+    pt, pb = _put(off, T), _put(off, B)
+    off.dtrsm(side, uplo, trans, diag, m, n, alpha, pt, kd, pb, m)
+    X = _get(off, pb, m, n)
+    R = opT @ X - alpha * B if side == "L" else X @ opT - alpha * B
+    nrm = np.abs(opT).sum(1).max() * np.abs(X).max() + abs(alpha) * np.abs(B).max()
+    assert np.abs(R).max() / nrm <= 2e-16, (side, uplo, trans, diag)
+    off.Free(pt)
+    off.Free(pb)
+
+
 @pytest.mark.parametrize("uplo", "LU")
 @pytest.mark.parametrize("n", [1, 63, 200])
 def test_dpotrf(off, uplo, n):
