@@ -1,8 +1,8 @@
 """Autotuner for the batched persistent factor + solve (ooc_batched_dposv / _sposv).
 
 The kernel's per-matrix panel width is the tuning knob: wide panels put more of the flops
-in the shared-memory trailing update, narrow ones need less shared memory and fewer
-synchronisations for small orders.  For each size bucket (n in [32 q, 32 q + 31]) the
+in the register-tiled trailing update (fewer passes over the trailing matrix), narrow ones
+shorten the serial diagonal-block and row-solve steps for small orders.  For each size bucket (n in [32 q, 32 q + 31]) the
 tuner times every candidate width on a synthetic batch of that bucket (A = M M^T / n + I,
 M ~ N(0, 1)), keeps the fastest, and persists the 16-entry table as JSON keyed by GPU
 name and precision:
@@ -20,7 +20,7 @@ import os
 import time
 
 NBUCKETS = 16
-CANDIDATES = {"fp64": (8, 16, 32), "fp32": (16, 32, 64)}
+CANDIDATES = {"fp64": (8, 16, 32), "fp32": (16, 32)}
 
 
 def default_path() -> str:

@@ -81,8 +81,9 @@ __device__ int chol32_warp(T* D, int off, int kb, int lane) {
   return bad;
 }
 
-// Shared layout: D[64][65] (diagonal block), P[NMAX][blk+1] (panel copy).  BLK is the
-// panel width (a compile-time constant, so that the panel solve keeps its row in registers).
+// FP64 factorization of one matrix by the CTA.  Shared layout: D[64][65] (diagonal block),
+// P[NMAX][blk+1] (panel copy).  BLK is the panel width (a compile-time constant, so that
+// the panel solve keeps its row in registers).
 template <typename T, int BLK>
 __device__ int factor_one(T* __restrict__ A, int n, T* D, T* P, int* s_fail) {
   constexpr int blk = BLK;
@@ -97,66 +98,24 @@ __device__ int factor_one(T* __restrict__ A, int n, T* D, T* P, int* s_fail) {
     }
     if (t == 0) *s_fail = 0;
     __syncthreads();
-    if constexpr (sizeof(T) == 4) {
-      // FP32: in one warp for kb <= 32; a wider block as two 32-blocks: L11 (warp), L21 := A21 L11^-T
-      // (a thread per row), A22 -= L21 L21^T (all threads), L22 (warp)
-      if (t < 32) {
-        const int b = chol32_warp(D, 0, min(kb, 32), t);
-        if (t == 0 && b < min(kb, 32)) *s_fail = k + b + 1;
+    // column by column over the CTA (a warp form would spill its doubles)
+    for (int j = 0; j < kb; j++) {
+      if (t == 0) {
+        const T d = D[j * 65 + j];
+        if (!(d > T(0))) *s_fail = k + j + 1;
+        else D[j * 65 + j] = tsqrt(d);
       }
       __syncthreads();
-      if (kb > 32 && !*s_fail) {
-        if (t >= 32 && t < kb) {
-          T v[32];
-#pragma unroll
-          for (int c = 0; c < 32; c++) v[c] = D[c * 65 + t];
-#pragma unroll
-          for (int c = 0; c < 32; c++) {
-            T x = v[c];
-#pragma unroll
-            for (int q = 0; q < c; q++) x -= v[q] * D[q * 65 + c];
-            v[c] = x / D[c * 65 + c];
-          }
-#pragma unroll
-          for (int c = 0; c < 32; c++) D[c * 65 + t] = v[c];
-        }
-        __syncthreads();
-        const int w2 = kb - 32;
-        for (int idx = t; idx < w2 * w2; idx += BT) {
-          const int c = 32 + idx / w2, r = 32 + idx % w2;
-          if (r >= c) {
-            T acc = T(0);
-#pragma unroll 8
-            for (int q = 0; q < 32; q++) acc += D[q * 65 + r] * D[q * 65 + c];
-            D[c * 65 + r] -= acc;
-          }
-        }
-        __syncthreads();
-        if (t < 32) {
-          const int b = chol32_warp(D, 32, w2, t);
-          if (t == 0 && b < w2) *s_fail = k + 32 + b + 1;
-        }
-        __syncthreads();
+      if (*s_fail) break;
+      const T inv = T(1) / D[j * 65 + j];
+      for (int r = j + 1 + t; r < kb; r += BT) D[j * 65 + r] *= inv;
+      __syncthreads();
+      const int w = kb - j - 1;
+      for (int idx = t; idx < w * w; idx += BT) {
+        const int c = j + 1 + idx / w, r = j + 1 + idx % w;
+        if (r >= c) D[c * 65 + r] -= D[j * 65 + r] * D[j * 65 + c];
       }
-    } else {  // FP64: column by column over the CTA (the warp form spills its doubles)
-      for (int j = 0; j < kb; j++) {
-        if (t == 0) {
-          const T d = D[j * 65 + j];
-          if (!(d > T(0))) *s_fail = k + j + 1;
-          else D[j * 65 + j] = tsqrt(d);
-        }
-        __syncthreads();
-        if (*s_fail) break;
-        const T inv = T(1) / D[j * 65 + j];
-        for (int r = j + 1 + t; r < kb; r += BT) D[j * 65 + r] *= inv;
-        __syncthreads();
-        const int w = kb - j - 1;
-        for (int idx = t; idx < w * w; idx += BT) {
-          const int c = j + 1 + idx / w, r = j + 1 + idx % w;
-          if (r >= c) D[c * 65 + r] -= D[j * 65 + r] * D[j * 65 + c];
-        }
-        __syncthreads();
-      }
+      __syncthreads();
     }
     for (int idx = t; idx < kb * kb; idx += BT) {
       const int c = idx / kb, r = idx % kb;
@@ -232,6 +191,137 @@ __device__ int factor_one(T* __restrict__ A, int n, T* D, T* P, int* s_fail) {
   return 0;
 }
 
+// FP32 factorization of one matrix by the CTA, in steps of BLK (16 or 32) columns:
+//   1. the diagonal block is factored by one warp in registers (chol32_warp), and the
+//      reciprocals of its diagonal are kept; from the second step on this happens inside
+//      the previous step's trailing update (warp 0 updates the block that holds it and
+//      factors it while the other warps update the rest);
+//   2. every row below solves against L_kk^T, one thread per row with the row in registers,
+//      right-looking (each column's FMAs independent of the others'); the result goes to
+//      the matrix and, transposed, to PT (PT[c ldt + i] = L(k + kb + i, k + c)), zero-padded
+//      to a multiple of 32 rows;
+//   3. the trailing lower triangle is updated by 32 x 32 blocks, a warp a block, each lane a
+//      4 x 8 register tile fed by 16-byte shared loads of PT (ten FMAs per shared load); the
+//      block's elements of the matrix are loaded before the products and stored after.
+// The trailing matrix stays in global memory (up to 1 MB per matrix); every element of it is
+// read and written once per step.
+__device__ __forceinline__ void bt_block_ij(int b, int& I, int& J) {
+  int i = (int)((sqrtf(8.f * (float)b + 1.f) - 1.f) * 0.5f);
+  if ((i + 1) * (i + 2) / 2 <= b) i++;
+  if (i * (i + 1) / 2 > b) i--;
+  I = i;
+  J = b - i * (i + 1) / 2;
+}
+
+template <int BLK>
+__device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int ldt, int* s_fail) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  float* rinv = D + 40 * 65;  // a column of D that a <= 32-wide block never uses
+  const int r0 = (lane & 7) * 4, c0 = (lane >> 3) * 8;
+  const int zero = n >> 30;  // n <= 512
+  // warp 0: factor the kb x kb diagonal block at column k (already in D), keep the
+  // reciprocals of its diagonal and write L_kk to the matrix
+  auto diag = [&](int k, int kb) {
+    const int b = chol32_warp(D, 0, kb, lane);
+    if (lane == 0) *s_fail = (b < kb) ? k + b + 1 : 0;
+    if (lane < BLK) rinv[lane] = (lane < kb) ? 1.f / D[lane * 65 + lane] : 0.f;
+    if (b == kb)
+      for (int idx = lane; idx < kb * kb; idx += 32) {
+        const int c = idx / kb, r = idx % kb;
+        if (r >= c) A[(k + r) + (i64)(k + c) * n] = D[c * 65 + r];
+      }
+  };
+  {
+    const int kb = min(BLK, n);
+    for (int idx = t; idx < kb * kb; idx += BT) {
+      const int c = idx / kb, r = idx % kb;
+      if (r >= c) D[c * 65 + r] = A[r + (i64)c * n];
+    }
+    __syncthreads();
+    if (warp == 0) diag(0, kb);
+    __syncthreads();
+  }
+  for (int k = 0; k < n; k += BLK) {
+    const int kb = min(BLK, n - k);
+    const int fail = *s_fail;
+    if (fail) return fail;
+    const int m = n - k - kb;
+    if (m <= 0) break;
+    const int m32 = (m + 31) & ~31;
+    for (int i = t; i < m32; i += BT) {
+      float r[BLK];
+      float* g = A + (k + kb + i);
+      const bool live = i < m;
+#pragma unroll
+      for (int c = 0; c < BLK; c++) r[c] = (live && c < kb) ? g[(i64)(k + c) * n] : 0.f;
+#pragma unroll
+      for (int c = 0; c < BLK; c++) {
+        r[c] *= rinv[c];
+        // zero at run time: column c's loads of L_kk wait for r[c] (not all hoisted into registers)
+        const float* lc = D + c * 65 + (zero & __float_as_int(r[c]));
+#pragma unroll
+        for (int q = c + 1; q < BLK; q++) r[q] = fmaf(-r[c], lc[q], r[q]);
+      }
+#pragma unroll
+      for (int c = 0; c < BLK; c++) {
+        const float v = (live && c < kb) ? r[c] : 0.f;
+        PT[c * ldt + i] = v;
+        if (live && c < kb) g[(i64)(k + c) * n] = v;
+      }
+    }
+    __syncthreads();
+    // Trailing update.  Warp 0 takes block (0, 0), which holds the next diagonal block: it
+    // also leaves that block's kn x kn corner in D and factors it at once, while warps
+    // 1.. update the other blocks; the next step's row solve follows the barrier directly.
+    const int nb32 = m32 >> 5, nblk = nb32 * (nb32 + 1) / 2;
+    const int kn = min(BLK, m);
+    float* C = A + (k + kb) + (i64)(k + kb) * n;
+    for (int b = (warp == 0) ? 0 : warp; b < nblk; b += (warp == 0) ? nblk : BT / 32 - 1) {
+      int I, J;
+      bt_block_ij(b, I, J);
+      const int rb = I * 32 + r0, cb = J * 32 + c0;
+      float cv[4][8];
+#pragma unroll
+      for (int ii = 0; ii < 4; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 8; jj++) {
+          const int row = rb + ii, col = cb + jj;
+          cv[ii][jj] = (row < m && col <= row) ? C[row + (i64)col * n] : 0.f;
+        }
+      float acc[4][8] = {};
+#pragma unroll 8
+      for (int q = 0; q < BLK; q++) {
+        const float4 a = *reinterpret_cast<const float4*>(PT + q * ldt + rb);
+        const float4 b0 = *reinterpret_cast<const float4*>(PT + q * ldt + cb);
+        const float4 b1 = *reinterpret_cast<const float4*>(PT + q * ldt + cb + 4);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int ii = 0; ii < 4; ii++)
+#pragma unroll
+          for (int jj = 0; jj < 8; jj++) acc[ii][jj] = fmaf(av[ii], bv[jj], acc[ii][jj]);
+      }
+#pragma unroll
+      for (int ii = 0; ii < 4; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 8; jj++) {
+          const int row = rb + ii, col = cb + jj;
+          if (row < m && col <= row) {
+            const float v = cv[ii][jj] - acc[ii][jj];
+            C[row + (i64)col * n] = v;
+            if (b == 0 && row < kn) D[col * 65 + row] = v;
+          }
+        }
+    }
+    if (warp == 0) {
+      __syncwarp();
+      diag(k + kb, kn);
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
 // L L^T x = b in place (b in global), blocks of 32 rows: one warp solves the diagonal
 // block with shuffles, all threads update the rest.
 template <typename T>
@@ -285,7 +375,7 @@ __device__ void solve_one(const T* __restrict__ L, int n, T* __restrict__ b) {
 // shared memory, sized per size class, lets two CTAs share an SM up to n = 256), 1 for FP64.
 template <typename T, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_batched_posv(const Item* __restrict__ items, int count, int* info,
-                                                           int* counter, int do_solve) {
+                                                           int* counter, int do_solve, int ldt) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   T* D = (T*)smem_raw;
   T* P = D + 64 * 65;
@@ -300,11 +390,15 @@ __global__ void __launch_bounds__(BT, MINB) k_batched_posv(const Item* __restric
     T* a = (T*)it.a;
     int f = 0;
     if (it.mode == 0) {
-      switch (it.blk) {  // the widths the autotuner chooses from (others fall back to 32)
-        case 8: f = factor_one<T, 8>(a, it.n, D, P, &s_fail); break;
-        case 16: f = factor_one<T, 16>(a, it.n, D, P, &s_fail); break;
-        case 64: f = factor_one<T, 64>(a, it.n, D, P, &s_fail); break;
-        default: f = factor_one<T, 32>(a, it.n, D, P, &s_fail); break;
+      if constexpr (sizeof(T) == 4) {  // 16- or 32-wide steps (the autotuner's choice)
+        if (it.blk <= 16) f = factor_f32<16>(a, it.n, D, P, ldt, &s_fail);
+        else f = factor_f32<32>(a, it.n, D, P, ldt, &s_fail);
+      } else {
+        switch (it.blk) {  // the widths the autotuner chooses from (others fall back to 32)
+          case 8: f = factor_one<T, 8>(a, it.n, D, P, &s_fail); break;
+          case 16: f = factor_one<T, 16>(a, it.n, D, P, &s_fail); break;
+          default: f = factor_one<T, 32>(a, it.n, D, P, &s_fail); break;
+        }
       }
     }
     if (threadIdx.x == 0) info[idx] = f;
@@ -320,8 +414,14 @@ __global__ void k_scatter_info(const int* sorted_info, const int* order, int cou
 }
 
 // Shared memory of a launch whose matrices have orders <= nmax and panel widths <= blk.
+// FP32 keeps the panel transposed (blk rows of ldt floats, ldt = the class's largest order
+// rounded up to 32, plus 4); FP64 keeps it row by row (nmax rows of blk + 1).
+inline int ldt_for(int nmax) { return (nmax + 31) / 32 * 32 + 4; }
 template <typename T>
-size_t smem_for(int blk, int nmax = NMAX) { return (size_t)(64 * 65 + nmax * (blk + 1)) * sizeof(T); }
+size_t smem_for(int blk, int nmax = NMAX) {
+  if (sizeof(T) == 4) return (size_t)(64 * 65 + std::min(blk, 32) * ldt_for(nmax)) * sizeof(T);
+  return (size_t)(64 * 65 + nmax * (blk + 1)) * sizeof(T);
+}
 template <typename T>
 constexpr int minb() { return sizeof(T) == 4 ? 2 : 1; }
 
@@ -356,8 +456,8 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
     const int j = order[i];
     const int bucket = std::min(NBUCKETS - 1, items_in[j].n / 32);
     int blk = blk_table ? blk_table[bucket] : (sizeof(T) == 8 ? 32 : 64);
-    blk = std::max(1, std::min(blk, sizeof(T) == 8 ? 32 : 64));
-    blk = blk <= 8 ? 8 : blk <= 16 ? 16 : blk <= 32 ? 32 : 64;  // the compiled widths
+    blk = std::max(1, std::min(blk, 32));
+    blk = sizeof(T) == 4 ? (blk <= 16 ? 16 : 32) : (blk <= 8 ? 8 : blk <= 16 ? 16 : 32);  // the compiled widths
     items[i] = items_in[j];
     items[i].blk = blk;
   }
@@ -421,7 +521,8 @@ int run_items(cudaStream_t s, int dev, std::vector<Item>& items_in, int* info_ho
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batched_posv<T, minb<T>()>, BT, sm);
       const int per = std::max(1, std::min(ctas_per_sm > 0 ? ctas_per_sm : occ, std::max(occ, 1)));
       const int grid = std::max(1, std::min(i1 - i0, nsm * per));
-      k_batched_posv<T, minb<T>()><<<grid, BT, sm, s>>>(d_items + i0, i1 - i0, d_info + i0, d_counter + ci, do_solve);
+      k_batched_posv<T, minb<T>()><<<grid, BT, sm, s>>>(d_items + i0, i1 - i0, d_info + i0, d_counter + ci, do_solve,
+                                                         ldt_for(cmax));
     }
     cudaEventRecord(e1, s);
     if (!rc) k_scatter_info<<<(count + 255) / 256, 256, 0, s>>>(d_info, d_order, count, d_out);

@@ -214,26 +214,33 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
   if (*(volatile int*)status) return;
   __shared__ double S[SB][SB + 1];  // S[col][row]
   __shared__ int failed;
+  __shared__ double s_inv;
   const int t = threadIdx.x;
-  for (int idx = t; idx < n * n; idx += blockDim.x) {
-    int c = idx / n, r = idx % n;
-    if (r >= c) S[c][r] = A[r + (i64)c * ld];
+  {  // 64 rows x 4 column groups: 16 loads in flight per thread
+    const int r = t & (SB - 1), cg = t >> 6;
+#pragma unroll
+    for (int i = 0; i < SB / 4; i++) {
+      const int c = cg + 4 * i;
+      if (r < n && c < n && r >= c) S[c][r] = A[r + (i64)c * ld];
+    }
   }
   if (t == 0) failed = 0;
   __syncthreads();
   for (int j = 0; j < n; j++) {
-    if (t == 0) {
+    if (t == 0) {  // one FP64 square root and one division per column, not one per thread
       double d = S[j][j];
       if (!(d > 0.0)) {
         failed = 1;
         atomicCAS(status, 0, (int)(col0 + j + 1));
       } else {
-        S[j][j] = sqrt(d);
+        const double sq = sqrt(d);
+        S[j][j] = sq;
+        s_inv = 1.0 / sq;
       }
     }
     __syncthreads();
     if (failed) break;
-    const double inv = 1.0 / S[j][j];
+    const double inv = s_inv;
     for (int r = j + 1 + t; r < n; r += blockDim.x) S[j][r] *= inv;
     __syncthreads();
     const int w = n - j - 1;  // trailing (w x w) lower triangle
@@ -293,11 +300,17 @@ __global__ void __launch_bounds__(TS_ROWS) k_trsm_small(const double* L, i64 ldl
   const int r0 = blockIdx.x * TS_ROWS;
   if (r0 >= mz) return;
   double* Bz = B + (i64)z * sB;
-  for (int idx = t; idx < SB * SB; idx += TS_ROWS) {
-    const int c = idx / SB, r = idx % SB;
-    double v = (r == c) ? 1.0 : 0.0;
-    if (r < n && c < n && r >= c) v = L[r + (i64)c * ldl];
-    Ls[idx] = v;
+  // L column by column, lanes down the rows: 16 loads in flight per thread (one warp
+  // cannot hide a load's latency one element at a time)
+#pragma unroll 8
+  for (int c = 0; c < SB; c++) {
+#pragma unroll
+    for (int h = 0; h < SB / TS_ROWS; h++) {
+      const int r = t + TS_ROWS * h;
+      double v = (r == c) ? 1.0 : 0.0;
+      if (r < n && c < n && r >= c) v = L[r + (i64)c * ldl];
+      Ls[c * SB + r] = v;
+    }
   }
   __syncthreads();
   for (int c = t; c < SB; c += TS_ROWS) Rinv[c] = 1.0 / Ls[c * SB + c];
