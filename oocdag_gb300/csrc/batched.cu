@@ -214,7 +214,7 @@ __device__ __forceinline__ void bt_block_ij(int b, int& I, int& J) {
 }
 
 template <int BLK>
-__device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int ldt, int* s_fail) {
+__device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int ldt, float* bs, int* s_fail) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   float* rinv = D + 40 * 65;  // a column of D that a <= 32-wide block never uses
   const int r0 = (lane & 7) * 4, c0 = (lane >> 3) * 8;
@@ -224,12 +224,24 @@ __device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int
   auto diag = [&](int k, int kb) {
     const int b = chol32_warp(D, 0, kb, lane);
     if (lane == 0) *s_fail = (b < kb) ? k + b + 1 : 0;
-    if (lane < BLK) rinv[lane] = (lane < kb) ? 1.f / D[lane * 65 + lane] : 0.f;
-    if (b == kb)
+    const float ri = (lane < kb) ? 1.f / D[lane * 65 + lane] : 0.f;
+    if (lane < BLK) rinv[lane] = ri;
+    if (b == kb) {
       for (int idx = lane; idx < kb * kb; idx += 32) {
         const int c = idx / kb, r = idx % kb;
         if (r >= c) A[(k + r) + (i64)(k + c) * n] = D[c * 65 + r];
       }
+      if (bs) {  // forward sweep, this block: y_k = L_kk^{-1} b_k (b_k is final: every
+                 // earlier step's row solve has already subtracted its panel's share)
+        float v = (lane < kb) ? bs[k + lane] : 0.f;
+        for (int j = 0; j < kb; j++) {
+          const float yj = __shfl_sync(0xffffffffu, v * ri, j);
+          if (lane == j) v = yj;
+          else if (lane > j) v = fmaf(-D[j * 65 + lane], yj, v);
+        }
+        if (lane < kb) bs[k + lane] = v;
+      }
+    }
   };
   {
     const int kb = min(BLK, n);
@@ -254,20 +266,22 @@ __device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int
       const bool live = i < m;
 #pragma unroll
       for (int c = 0; c < BLK; c++) r[c] = (live && c < kb) ? g[(i64)(k + c) * n] : 0.f;
+      float fw = 0.f;  // forward sweep: b_i -= L(i, k..) y_k (y_k sits in bs[k..])
+      const float* yk = bs ? bs + k : rinv;
 #pragma unroll
       for (int c = 0; c < BLK; c++) {
         r[c] *= rinv[c];
         // zero at run time: column c's loads of L_kk wait for r[c] (not all hoisted into registers)
-        const float* lc = D + c * 65 + (zero & __float_as_int(r[c]));
+        const int z = zero & __float_as_int(r[c]);
+        const float* lc = D + c * 65 + z;
 #pragma unroll
         for (int q = c + 1; q < BLK; q++) r[q] = fmaf(-r[c], lc[q], r[q]);
-      }
-#pragma unroll
-      for (int c = 0; c < BLK; c++) {
         const float v = (live && c < kb) ? r[c] : 0.f;
         PT[c * ldt + i] = v;
         if (live && c < kb) g[(i64)(k + c) * n] = v;
+        if (c < kb) fw = fmaf(v, yk[c + z], fw);  // never reads past the vector
       }
+      if (bs && live) bs[k + kb + i] -= fw;
     }
     __syncthreads();
     // Trailing update.  Warp 0 takes block (0, 0), which holds the next diagonal block: it
@@ -320,6 +334,39 @@ __device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int
     __syncthreads();
   }
   return 0;
+}
+
+// Backward sweep L^T x = y for the vector in shared memory (FP32 path; the forward sweep
+// ran inside the factorization): blocks of 32 rows from the last, one warp solves the
+// diagonal block with shuffles, all threads take the block's share off the rows above.
+__device__ void solve_back_f32(const float* __restrict__ L, int n, float* bs) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int k = ((n - 1) / 32) * 32; k >= 0; k -= 32) {
+    const int kb = min(32, n - k);
+    if (warp == 0) {
+      float v = (lane < kb) ? bs[k + lane] : 0.f;
+      const float ljj = (lane < kb) ? L[(k + lane) + (i64)(k + lane) * n] : 1.f;
+      for (int j = kb - 1; j >= 0; j--) {
+        const float xj = __shfl_sync(0xffffffffu, v / ljj, j);
+        if (lane == j) v = xj;
+        else if (lane < j) v = fmaf(-L[(k + j) + (i64)(k + lane) * n], xj, v);  // (L^T)(lane, j) = L(j, lane)
+      }
+      if (lane < kb) bs[k + lane] = v;
+    }
+    __syncthreads();
+    for (int i = t; i < k; i += BT) {
+      const float* li = L + k + (i64)i * n;  // L(k.., i): contiguous rows of column i
+      float s0 = 0.f, s1 = 0.f;
+#pragma unroll 8
+      for (int j = 0; j + 1 < kb; j += 2) {
+        s0 = fmaf(li[j], bs[k + j], s0);
+        s1 = fmaf(li[j + 1], bs[k + j + 1], s1);
+      }
+      if (kb & 1) s0 = fmaf(li[kb - 1], bs[k + kb - 1], s0);
+      bs[i] -= s0 + s1;
+    }
+    __syncthreads();
+  }
 }
 
 // L L^T x = b in place (b in global), blocks of 32 rows: one warp solves the diagonal
@@ -389,10 +436,23 @@ __global__ void __launch_bounds__(BT, MINB) k_batched_posv(const Item* __restric
     const Item it = items[idx];
     T* a = (T*)it.a;
     int f = 0;
+    bool solved = false;
     if (it.mode == 0) {
       if constexpr (sizeof(T) == 4) {  // 16- or 32-wide steps (the autotuner's choice)
-        if (it.blk <= 16) f = factor_f32<16>(a, it.n, D, P, ldt, &s_fail);
-        else f = factor_f32<32>(a, it.n, D, P, ldt, &s_fail);
+        // the right-hand side in shared memory: the forward sweep runs inside the
+        // factorization, the backward sweep after it
+        float* bs = do_solve ? P + 32 * ldt : nullptr;
+        if (bs) {
+          for (int i = threadIdx.x; i < it.n; i += BT) bs[i] = ((const float*)it.b)[i];
+          __syncthreads();
+        }
+        if (it.blk <= 16) f = factor_f32<16>(a, it.n, D, P, ldt, bs, &s_fail);
+        else f = factor_f32<32>(a, it.n, D, P, ldt, bs, &s_fail);
+        if (bs && f == 0) {
+          solve_back_f32(a, it.n, bs);
+          for (int i = threadIdx.x; i < it.n; i += BT) ((float*)it.b)[i] = bs[i];
+        }
+        solved = true;
       } else {
         switch (it.blk) {  // the widths the autotuner chooses from (others fall back to 32)
           case 8: f = factor_one<T, 8>(a, it.n, D, P, &s_fail); break;
@@ -402,7 +462,7 @@ __global__ void __launch_bounds__(BT, MINB) k_batched_posv(const Item* __restric
       }
     }
     if (threadIdx.x == 0) info[idx] = f;
-    if (f == 0 && do_solve) solve_one<T>(a, it.n, (T*)it.b);
+    if (f == 0 && do_solve && !solved) solve_one<T>(a, it.n, (T*)it.b);
     __syncthreads();
   }
 }
@@ -414,12 +474,13 @@ __global__ void k_scatter_info(const int* sorted_info, const int* order, int cou
 }
 
 // Shared memory of a launch whose matrices have orders <= nmax and panel widths <= blk.
-// FP32 keeps the panel transposed (blk rows of ldt floats, ldt = the class's largest order
-// rounded up to 32, plus 4); FP64 keeps it row by row (nmax rows of blk + 1).
+// FP32 keeps the panel transposed (up to 32 rows of ldt floats, ldt = the class's largest
+// order rounded up to 32, plus 4) and the right-hand side (ldt floats); FP64 keeps the
+// panel row by row (nmax rows of blk + 1).
 inline int ldt_for(int nmax) { return (nmax + 31) / 32 * 32 + 4; }
 template <typename T>
 size_t smem_for(int blk, int nmax = NMAX) {
-  if (sizeof(T) == 4) return (size_t)(64 * 65 + std::min(blk, 32) * ldt_for(nmax)) * sizeof(T);
+  if (sizeof(T) == 4) return (size_t)(64 * 65 + 33 * ldt_for(nmax)) * sizeof(T);  // D, PT (<= 32 rows), b
   return (size_t)(64 * 65 + nmax * (blk + 1)) * sizeof(T);
 }
 template <typename T>
