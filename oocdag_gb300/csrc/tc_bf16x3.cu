@@ -799,8 +799,30 @@ __device__ __forceinline__ void umma_bf16_n256(uint32_t tmem_d, uint64_t da, uin
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(da), "l"(db), "r"(IDESC_N256), "r"(accumulate));
 }
+// Operand ring of the transposed kernel: four stages of K = 32 (64-byte rows, 64-byte
+// swizzle), 48 KB each, where the K = 64 kernels hold two stages of 96 KB: the same bytes
+// in flight, but the MMA can start on a stage as soon as half as many bytes have landed
+// and the producer refills a stage after half as many MMAs.
+constexpr int TK_T = 32;
+constexpr int STAGES_T = 4;
+constexpr int A_T_PLANE = TM2 * TK_T * 2;                      // 16 KB
+constexpr int B_T_PLANE = TB * TK_T * 2;                       // 8 KB
+constexpr int STAGE_T_BYTES = 2 * A_T_PLANE + 2 * B_T_PLANE;   // 48 KB
+static_assert(STAGES_T * STAGE_T_BYTES == STAGES2 * STAGE2_BYTES, "the transposed ring keeps the smem budget");
+static_assert(A_T_PLANE % 512 == 0 && B_T_PLANE % 512 == 0, "64-byte swizzle atoms are 512-byte aligned");
+// Shared-memory matrix descriptor for a K-major BF16 tile with the 64-byte swizzle: rows
+// of 64 bytes, 8-row atoms of 512 bytes one after another along M/N.
+__device__ __forceinline__ uint64_t umma_desc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)(16 >> 4) << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;                  // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                           // fixed 0b001
+  d |= (uint64_t)4 << 61;                           // 64-byte swizzle
+  return d;
+}
 constexpr int TBOX = 32;  // 32 x 32 FP32 C boxes (4 KB, 1024-byte aligned for the swizzle)
-constexpr int BOX2T_OFF = STAGES2 * STAGE2_BYTES + 1024;  // after the control block, padded
+constexpr int BOX2T_OFF = STAGES_T * STAGE_T_BYTES + 1024;  // after the control block, padded
 constexpr int SMEM2T_BYTES = BOX2T_OFF + EPI2_WARPS * TBOX * TBOX * 4 + 1024 /*align*/;  // 231,424
 static_assert(SMEM2T_BYTES <= 232448, "transposed update kernel shared memory");
 
@@ -812,24 +834,24 @@ __global__ void __launch_bounds__(THREADS2, 1)
   if (*(volatile int*)status) return;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
-  uint64_t* empty = full + STAGES2;
-  uint64_t* tfull = empty + STAGES2;
+  uint64_t* full = (uint64_t*)(smem + STAGES_T * STAGE_T_BYTES);
+  uint64_t* empty = full + STAGES_T;
+  uint64_t* tfull = empty + STAGES_T;
   uint64_t* tempty = tfull + NSLOT2;
   uint64_t* done = tempty + NSLOT2;
   uint32_t* tmem_slot = (uint32_t*)(done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-  volatile long long* n_issued = (volatile long long*)(smem + STAGES2 * STAGE2_BYTES + 128);
+  volatile long long* n_issued = (volatile long long*)(smem + STAGES_T * STAGE_T_BYTES + 128);
   volatile long long* n_consumed = n_issued + 1;
-  uint64_t* idfull = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES + 160);
+  uint64_t* idfull = (uint64_t*)(smem + STAGES_T * STAGE_T_BYTES + 160);
   uint64_t* idempty = idfull + NID2;
   volatile long long* ids = (volatile long long*)(idempty + NID2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = Kp / TK;
+  const int nk = Kp / TK_T;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES2; s++) {
+    for (int s = 0; s < STAGES_T; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -880,18 +902,18 @@ __global__ void __launch_bounds__(THREADS2, 1)
       const bool b_in_a = (bj == 2 * bi2 || bj == 2 * bi2 + 1);
       for (int kc = 0; kc < nk; kc++, c++) {
         if (lane == 0) {
-          const int s = (int)(c % STAGES2);
-          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          const int s = (int)(c % STAGES_T);
+          const uint32_t ph = (uint32_t)((c / STAGES_T) & 1);
           if (!mbar_wait(&empty[s], ph ^ 1, abort_flag)) {
             ok = false;
           } else {
-            uint8_t* st = smem + s * STAGE2_BYTES;
-            mbar_expect_tx(&full[s], b_in_a ? 2 * A2_PLANE : STAGE2_BYTES);
-            tma_load_2d(st, &map_ahi, &full[s], kc * TK, bi2 * TM2);
-            tma_load_2d(st + A2_PLANE, &map_alo, &full[s], kc * TK, bi2 * TM2);
+            uint8_t* st = smem + s * STAGE_T_BYTES;
+            mbar_expect_tx(&full[s], b_in_a ? 2 * A_T_PLANE : STAGE_T_BYTES);
+            tma_load_2d(st, &map_ahi, &full[s], kc * TK_T, bi2 * TM2);
+            tma_load_2d(st + A_T_PLANE, &map_alo, &full[s], kc * TK_T, bi2 * TM2);
             if (!b_in_a) {
-              tma_load_2d(st + 2 * A2_PLANE, &map_bhi, &full[s], kc * TK, bj * TB);
-              tma_load_2d(st + 2 * A2_PLANE + B2_PLANE, &map_blo, &full[s], kc * TK, bj * TB);
+              tma_load_2d(st + 2 * A_T_PLANE, &map_bhi, &full[s], kc * TK_T, bj * TB);
+              tma_load_2d(st + 2 * A_T_PLANE + B_T_PLANE, &map_blo, &full[s], kc * TK_T, bj * TB);
             }
             *n_issued = c + 1;
           }
@@ -924,24 +946,24 @@ __global__ void __launch_bounds__(THREADS2, 1)
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
         const uint32_t d = tmem + (uint32_t)(slot * 2 * TB);
         for (int kc = 0; kc < nk; kc++, c++) {
-          const int s = (int)(c % STAGES2);
-          const uint32_t ph = (uint32_t)((c / STAGES2) & 1);
+          const int s = (int)(c % STAGES_T);
+          const uint32_t ph = (uint32_t)((c / STAGES_T) & 1);
           if (!mbar_wait(&full[s], ph, abort_flag)) { ok = false; break; }
           *n_consumed = c + 1;
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-          const uint32_t base = smem_u32(smem + s * STAGE2_BYTES);
-          const uint32_t a_hi = base, a_lo = base + A2_PLANE;
-          const uint32_t half_b = (uint32_t)(TB * 128);
-          uint32_t b_hi = base + 2 * A2_PLANE, b_lo = base + 2 * A2_PLANE + B2_PLANE;
+          const uint32_t base = smem_u32(smem + s * STAGE_T_BYTES);
+          const uint32_t a_hi = base, a_lo = base + A_T_PLANE;
+          const uint32_t half_b = (uint32_t)(TB * TK_T * 2);
+          uint32_t b_hi = base + 2 * A_T_PLANE, b_lo = base + 2 * A_T_PLANE + B_T_PLANE;
           if (bj == 2 * bi2) { b_hi = a_hi; b_lo = a_lo; }
           if (bj == 2 * bi2 + 1) { b_hi = a_hi + half_b; b_lo = a_lo + half_b; }
 #pragma unroll
-          for (int kk = 0; kk < TK / 16; kk++) {
+          for (int kk = 0; kk < TK_T / 16; kk++) {
             const uint32_t off = kk * 32;
             const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
-            umma_bf16_n256(d, umma_desc_sw128(b_hi + off), umma_desc_sw128(a_hi + off), acc0);
-            umma_bf16_n256(d, umma_desc_sw128(b_hi + off), umma_desc_sw128(a_lo + off), 1u);
-            umma_bf16_n256(d, umma_desc_sw128(b_lo + off), umma_desc_sw128(a_hi + off), 1u);
+            umma_bf16_n256(d, umma_desc_sw64(b_hi + off), umma_desc_sw64(a_hi + off), acc0);
+            umma_bf16_n256(d, umma_desc_sw64(b_hi + off), umma_desc_sw64(a_lo + off), 1u);
+            umma_bf16_n256(d, umma_desc_sw64(b_lo + off), umma_desc_sw64(a_hi + off), 1u);
           }
           umma_commit(&empty[s]);
         }
@@ -1034,7 +1056,7 @@ __global__ void __launch_bounds__(THREADS2, 1)
     }
     if (warp == 0 && lane == 0) {
       for (long long c = *n_consumed; c < *n_issued; c++)
-        (void)mbar_wait(&full[c % STAGES2], (uint32_t)((c / STAGES2) & 1), nullptr);
+        (void)mbar_wait(&full[c % STAGES_T], (uint32_t)((c / STAGES_T) & 1), nullptr);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -1310,15 +1332,16 @@ int get_encode() {
 }
 
 // BF16 plane of `rows` rows of K values (row-major, `ldk` elements between rows; ldk = K
-// when omitted): boxes of TK x box_rows.  Rows and K past the plane read as zeros.
-int make_map(CUtensorMap* map, void* base, int rows, int K, int box_rows = TB, i64 ldk = 0) {
+// when omitted): boxes of TK x box_rows, 128-byte swizzle (or TK_T x box_rows with the
+// 64-byte swizzle for the transposed kernel's ring).  Rows and K past the plane read as zeros.
+int make_map(CUtensorMap* map, void* base, int rows, int K, int box_rows = TB, i64 ldk = 0, bool k32 = false) {
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ldk > 0 ? ldk : K) * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)(k32 ? TK_T : TK), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, k32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? OOC_OK : OOC_ERR_CUDA;
 }
 
@@ -1544,16 +1567,17 @@ int launch_syrk_planes_f32(const void* hi, const void* lo, i64 ldk, int m, int K
   int dev = 0, nsm = 0;
   OOC_CUDA_TRY(cudaGetDevice(&dev));
   OOC_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const bool c16 = reinterpret_cast<uintptr_t>(C) % 16 == 0 && (ldc * (i64)sizeof(float)) % 16 == 0;
+  // long K (catch-ups): the transposed N=256 kernel with its K=32 ring; short K: the K=512-tuned one
+  const bool tr = c16 && K >= kLongK;
   CUtensorMap mh, ml;
-  if (make_map(&mh, h, m, K, TB, ldk) || make_map(&ml, l, m, K, TB, ldk)) {
+  if (make_map(&mh, h, m, K, TB, ldk, tr) || make_map(&ml, l, m, K, TB, ldk, tr)) {
     ooc_set_last_message("cuTensorMapEncodeTiled failed for the plane-store window");
     return OOC_ERR_CUDA;
   }
-  if (reinterpret_cast<uintptr_t>(C) % 16 == 0 && (ldc * (i64)sizeof(float)) % 16 == 0) {
-    // long K (catch-ups): the transposed N=256 kernel; short K: the K=512-tuned one
-    const bool tr = K >= kLongK;
+  if (c16) {
     CUtensorMap ah, al, mc;
-    if (make_map(&ah, h, m, K, TM2, ldk) || make_map(&al, l, m, K, TM2, ldk) ||
+    if (make_map(&ah, h, m, K, TM2, ldk, tr) || make_map(&al, l, m, K, TM2, ldk, tr) ||
         (tr ? make_map_c32t(&mc, C, m, ldc) : make_map_c32(&mc, C, m, ldc))) {
       ooc_set_last_message("cuTensorMapEncodeTiled failed for the update operands");
       return OOC_ERR_CUDA;

@@ -80,6 +80,35 @@ def test_mix_equals_alone_and_reaches_tolerance(ooc):
         assert paths == {0, 1, 2}  # the batched kernel, the pipelines and the out-of-core route
 
 
+def test_large_orders_mix_equals_alone(ooc):
+    # Orders up to 16384 in HBM (no out-of-core route): four pipelines factor and refine them
+    # side by side with a stream of small batched systems; each solution must be bit-identical
+    # to the one the same request gets alone, and reach the backward-error bar.
+    from oocdag_gb300.server import Server
+
+    rng = np.random.default_rng(11)
+    reqs = [dict(n=n, matrix_seed=2000 + i, rhs_seed=6000 + i, key=i, kind=0)
+            for i, n in enumerate([4096, 16384, 6000, 9999, 12288, 3000, 8192, 5000])]
+    reqs += [dict(n=int(rng.integers(32, 512)), matrix_seed=3000 + i, rhs_seed=7000 + i, key=100 + i, kind=0)
+             for i in range(24)]
+    alone = {}
+    with Server(workers=4, nb=512, prec="bf16x3", batch_window_ms=0.2) as S:
+        for q in reqs:
+            rid = S.submit(keep_solution=True, **q)
+            c = _drain(S, [rid], timeout_s=300.0)[rid]
+            assert c["status"] == 0 and c["info"] == 0, (c, S.last_error())
+            alone[q["key"]] = S.solution(rid, q["n"])
+    with Server(workers=4, nb=512, prec="bf16x3", batch_window_ms=2.0) as S:
+        ids = {S.submit(keep_solution=True, **q): q for q in reqs}
+        done = _drain(S, list(ids), timeout_s=300.0)
+        for rid, q in ids.items():
+            c = done[rid]
+            assert c["status"] == 0 and c["info"] == 0, (c, S.last_error())
+            assert c["backward_error"] <= BERR_TOL, c
+            np.testing.assert_array_equal(S.solution(rid, q["n"]), alone[q["key"]])
+        assert {c["path"] for c in done.values()} == {0, 1}
+
+
 def test_refuses_requests_that_never_fit(ooc):
     from oocdag_gb300.server import Server
 
