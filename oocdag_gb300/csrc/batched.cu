@@ -337,33 +337,48 @@ __device__ int factor_f32(float* __restrict__ A, int n, float* D, float* PT, int
 }
 
 // Backward sweep L^T x = y for the vector in shared memory (FP32 path; the forward sweep
-// ran inside the factorization): blocks of 32 rows from the last, one warp solves the
-// diagonal block with shuffles, all threads take the block's share off the rows above.
+// ran inside the factorization), blocks of 32 rows from the last.  Once x_K is known,
+// warp 0 takes its share off the rows of block K-1 and solves that block at once (a
+// 32 x 32 triangular system with shuffles), while the other warps take x_K's share off the
+// rows above; one barrier per block.  Every row receives the same subtractions in the same
+// order whichever warp performs them.
+__device__ __forceinline__ void back_share(const float* __restrict__ L, int n, float* bs, int k, int kb, int i) {
+  const float* li = L + k + (i64)i * n;  // L(k.., i): contiguous rows of column i
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll 8
+  for (int j = 0; j + 1 < kb; j += 2) {
+    s0 = fmaf(li[j], bs[k + j], s0);
+    s1 = fmaf(li[j + 1], bs[k + j + 1], s1);
+  }
+  if (kb & 1) s0 = fmaf(li[kb - 1], bs[k + kb - 1], s0);
+  bs[i] -= s0 + s1;
+}
+
+__device__ __forceinline__ void back_block(const float* __restrict__ L, int n, float* bs, int k, int lane) {
+  const int kb = min(32, n - k);
+  float v = (lane < kb) ? bs[k + lane] : 0.f;
+  const float ljj = (lane < kb) ? L[(k + lane) + (i64)(k + lane) * n] : 1.f;
+  for (int j = kb - 1; j >= 0; j--) {
+    const float xj = __shfl_sync(0xffffffffu, v / ljj, j);
+    if (lane == j) v = xj;
+    else if (lane < j) v = fmaf(-L[(k + j) + (i64)(k + lane) * n], xj, v);  // (L^T)(lane, j) = L(j, lane)
+  }
+  if (lane < kb) bs[k + lane] = v;
+}
+
 __device__ void solve_back_f32(const float* __restrict__ L, int n, float* bs) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  for (int k = ((n - 1) / 32) * 32; k >= 0; k -= 32) {
+  int k = ((n - 1) / 32) * 32;
+  if (warp == 0) back_block(L, n, bs, k, lane);
+  __syncthreads();
+  for (; k > 0; k -= 32) {  // x for rows k.. is final
     const int kb = min(32, n - k);
     if (warp == 0) {
-      float v = (lane < kb) ? bs[k + lane] : 0.f;
-      const float ljj = (lane < kb) ? L[(k + lane) + (i64)(k + lane) * n] : 1.f;
-      for (int j = kb - 1; j >= 0; j--) {
-        const float xj = __shfl_sync(0xffffffffu, v / ljj, j);
-        if (lane == j) v = xj;
-        else if (lane < j) v = fmaf(-L[(k + j) + (i64)(k + lane) * n], xj, v);  // (L^T)(lane, j) = L(j, lane)
-      }
-      if (lane < kb) bs[k + lane] = v;
-    }
-    __syncthreads();
-    for (int i = t; i < k; i += BT) {
-      const float* li = L + k + (i64)i * n;  // L(k.., i): contiguous rows of column i
-      float s0 = 0.f, s1 = 0.f;
-#pragma unroll 8
-      for (int j = 0; j + 1 < kb; j += 2) {
-        s0 = fmaf(li[j], bs[k + j], s0);
-        s1 = fmaf(li[j + 1], bs[k + j + 1], s1);
-      }
-      if (kb & 1) s0 = fmaf(li[kb - 1], bs[k + kb - 1], s0);
-      bs[i] -= s0 + s1;
+      back_share(L, n, bs, k, kb, k - 32 + lane);
+      __syncwarp();
+      back_block(L, n, bs, k - 32, lane);
+    } else {
+      for (int i = t - 32; i < k - 32; i += BT - 32) back_share(L, n, bs, k, kb, i);
     }
     __syncthreads();
   }
