@@ -78,7 +78,7 @@ enum {
                               synchronises the device); released by ooc_destroy, or when
                               an allocation fails.  Default 40 % of device memory, 0 =
                               no caching.                                             */
-  OOC_OPT_BLOCK_COLS = 9   /* split-BF16 factors of a stored matrix (nb a multiple of
+  OOC_OPT_BLOCK_COLS = 9,  /* split-BF16 factors of a stored matrix (nb a multiple of
                               128): width, in columns (rounded up to whole panels), of the
                               left-looking column blocks.  A block is caught up with every
                               finished panel by long-K tensor-core updates, then factored
@@ -90,6 +90,9 @@ enum {
                               = 4096 for device and page-locked host matrices with
                               n > 8192, 0 otherwise.  Needs a plane store of 4 n^2
                               device bytes while the factor is computed.              */
+  OOC_OPT_COPY_STREAMS = 10 /* host-to-device streams a streamed host matrix's column
+                              chunks alternate over (1 or 2; default 1); two keep two
+                              copy engines in flight                                 */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */
@@ -101,7 +104,8 @@ const char* ooc_last_error_string(void);
 /* LAPACK info of the last factorization run on the handle. */
 int ooc_last_info(ooc_handle* h);
 /* The handle's CUDA streams (which: 0 = compute, 1 = host-to-device copies,
- * 2 = device-to-host copies), as a cudaStream_t, so that a caller can order its own
+ * 2 = device-to-host copies, 3 = a second host-to-device copy stream that streamed host
+ * matrices use beside the first), as a cudaStream_t, so that a caller can order its own
  * work or timing events against the library's.
  * Device-pointer arguments are read on these streams (compute and host-to-device)
  * from the moment of the call: data still being produced on another stream must be

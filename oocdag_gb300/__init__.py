@@ -38,6 +38,7 @@ OPT_KEEP_A = 6
 OPT_TAIL_ORDER = 7
 OPT_POOL_BYTES = 8
 OPT_BLOCK_COLS = 9
+OPT_COPY_STREAMS = 10
 
 PREC_FP64 = 0
 PREC_FP32 = 1

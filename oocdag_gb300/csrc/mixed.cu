@@ -2099,8 +2099,11 @@ struct LbSource {
 // every finished column, then the in-core factorization; here a block of whole panels).
 // Block b covers columns [c0, c1); F_b is its first panel, F_{b+1} the next block's.
 //   sc  copies the host matrix's lower triangle, chunk after chunk in column order, as
-//       far ahead as the staging allows (all of it when a kept copy is the destination);
-//   s0  converts each chunk to FP32 when it is needed.  At block b's start F_b is already
+//       far ahead as the staging allows (all of it when a kept copy is the destination),
+//       and, for a device matrix or a kept copy, converts each group of columns to FP32
+//       right behind its copies (beside s0's tensor-core work);
+//   s0  converts staged chunks to FP32 when they are needed, or waits for the group's
+//       conversion on sc.  At block b's start F_b is already
 //       up to date, so s1 factors its diagonal tile at once while s0 catches the rest of
 //       the block and F_{b+1} up with all panels before the block (long-K tensor-core
 //       updates from the plane store, at most kCatchK columns of K per launch).  The
@@ -2117,7 +2120,7 @@ struct LbSource {
 // Requires the tensor-core column solve (nb and nb2 multiples of 128).
 constexpr i64 kCatchK = 8192;
 
-int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t sc, i64 block_cols,
+int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t sc, cudaStream_t sc2, i64 block_cols,
                   const LbSource& src, int64_t* launches, MixedProf* prof) {
   const i64 n = F->n;
   const int nb = F->nb;
@@ -2202,8 +2205,14 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
   int next_copy = 0, next_conv = 0;
   OOC_CUDA_TRY(cudaEventRecord(evP, s0));  // the factor's buffers were set up on s0
   OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evP, 0));
+  // Device matrices and kept host copies ("side" mode): the copies and every conversion
+  // run on sc, group after group in the order the compute stream needs them, so the
+  // conversions (HBM-bound) overlap the compute stream's tensor-core work; s0 only waits
+  // for a group's event before it uses the group's columns.  A group is F_0, then for each
+  // block the rest of its panels and the next block's first panel.
+  const bool side = src.on_device || src.keep;
   auto enqueue_copies = [&]() -> int {
-    if (src.on_device) return OOC_OK;
+    if (src.on_device || side) return OOC_OK;
     while (next_copy < nchunks && (src.keep || next_copy < next_conv + src.slots)) {
       const Chunk& c = chunks[next_copy];
       double* dst;
@@ -2257,8 +2266,57 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
   // panels q0..q1 into the FP32 matrix: one conversion over their columns (a device
   // matrix, or the kept copy once its last chunk has arrived), or chunk by chunk through
   // the staging slots
+  std::vector<int> group_of(bb, -1);
+  std::vector<cudaEvent_t> evConv, evCopy2;
+  if (side) {
+    OOC_CUDA_TRY(cudaStreamWaitEvent(sc2, evP, 0));
+    std::vector<std::pair<int, int>> groups{{0, 0}};
+    for (const auto& bk : blocks) {
+      const int q1 = std::min(bk.second, bb - 1);
+      if (q1 >= bk.first + 1) groups.emplace_back(bk.first + 1, q1);
+    }
+    evConv.resize(groups.size());
+    evCopy2.resize(groups.size());
+    for (size_t g = 0; g < groups.size(); g++) {
+      const int q0 = groups[g].first, q1 = groups[g].second;
+      for (int q = q0; q <= q1; q++) group_of[q] = (int)g;
+      if ((rc = new_event(&evConv[g])) || (rc = new_event(&evCopy2[g]))) return rc;
+      if (!src.on_device) {  // this group's chunks into the kept FP64 copy, in column order,
+                             // alternately on the two copy streams (two copy engines in flight)
+        if (prof->on && g == 0) {
+          OOC_CUDA_TRY(cudaEventCreate(&prof->h2d0));
+          OOC_CUDA_TRY(cudaEventRecord(prof->h2d0, sc));
+          OOC_CUDA_TRY(cudaStreamWaitEvent(sc2, prof->h2d0, 0));
+        }
+        for (int k = panel_chunks[q0].first; k < panel_chunks[q1].second; k++) {
+          const Chunk& c = chunks[k];
+          OOC_CUDA_TRY(cudaMemcpy2DAsync(src.keep + c.c0 + c.c0 * n, n * sizeof(double), src.A + c.c0 + c.c0 * src.lda,
+                                         src.lda * sizeof(double), (n - c.c0) * sizeof(double), c.c1 - c.c0,
+                                         cudaMemcpyHostToDevice, (k & 1) ? sc2 : sc));
+          prof->h2d_bytes += (double)(n - c.c0) * (double)(c.c1 - c.c0) * sizeof(double);
+        }
+        OOC_CUDA_TRY(cudaEventRecord(evCopy2[g], sc2));  // sc converts after both streams' copies
+        OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evCopy2[g], 0));
+        if (prof->on && panel_chunks[q1].second == nchunks) {
+          OOC_CUDA_TRY(cudaEventCreate(&prof->h2d1));
+          OOC_CUDA_TRY(cudaEventRecord(prof->h2d1, sc));
+        }
+      }
+      const i64 c0 = col_of(q0), c1 = col_of(q1 + 1);
+      const double* from = src.on_device ? src.A + c0 * src.lda : src.keep + c0 * n;
+      k_lower_conv<double, float><<<dim3(gx, (unsigned)std::min<i64>(c1 - c0, 1024)), 256, 0, sc>>>(
+          from, src.on_device ? src.lda : n, A + c0 * lda, lda, n, c0, (int)(c1 - c0), 0);
+      OOC_CUDA_TRY(cudaGetLastError());
+      OOC_CUDA_TRY(cudaEventRecord(evConv[g], sc));
+      if (launches) *launches += 1;
+    }
+  }
   auto convert_panels = [&](int q0, int q1) -> int {
     if (q1 < q0) return OOC_OK;
+    if (side) {  // converted on sc: wait for the group that holds them
+      OOC_CUDA_TRY(cudaStreamWaitEvent(s0, evConv[group_of[q1]], 0));
+      return OOC_OK;
+    }
     if (src.on_device || src.keep) {
       const int k1 = panel_chunks[q1].second - 1;
       const i64 c0 = col_of(q0), c1 = col_of(q1 + 1);
@@ -2520,7 +2578,11 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
     ooc_get_stream(h, 1, &s1p);
     if (lb) {
       void* s2p = nullptr;
+      void* s3p = nullptr;
       ooc_get_stream(h, 2, &s2p);
+      int64_t ncs = 1;
+      ooc_get_option(h, OOC_OPT_COPY_STREAMS, &ncs);
+      ooc_get_stream(h, ncs > 1 ? 3 : 2, &s3p);  // one stream: sc2 is sc itself
       LbSource src;
       src.A = A;
       src.lda = lda;
@@ -2532,7 +2594,7 @@ static int create_impl(ooc_handle* h, const double* A, int64_t n, int64_t lda, b
         rc = stage.ensure((size_t)src.slots * (size_t)n * (size_t)src.chunk * sizeof(double));
         src.stage = (double*)stage.p;
       }
-      if (!rc) rc = factor_f32_lb(F, s, (cudaStream_t)s1p, (cudaStream_t)s2p, bcols, src, &launches, &prof);
+      if (!rc) rc = factor_f32_lb(F, s, (cudaStream_t)s1p, (cudaStream_t)s2p, (cudaStream_t)s3p, bcols, src, &launches, &prof);
     } else {
       rc = reduced ? factor_f32(F, prec, s, (cudaStream_t)s1p, &launches, &prof)
                    : factor_mixed(F, prec, s, (cudaStream_t)s1p, &launches, &prof);

@@ -59,6 +59,7 @@ extern "C" const char* ooc_last_error_string(void) { return g_last_error.c_str()
 struct ooc_handle {
   int device = 0;
   cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
+  cudaStream_t s_h2d2 = nullptr;  // a second host-to-device copy stream (two copy engines in flight)
   int* d_status = nullptr;
   int* h_status = nullptr;  // page-locked mirror
   double* d_buf = nullptr;
@@ -71,6 +72,7 @@ struct ooc_handle {
   int keep_a = 0;
   int64_t tail_order = 24576;
   int64_t block_cols = -1;  // OOC_OPT_BLOCK_COLS (-1: by input)
+  int copy_streams = 1;      // OOC_OPT_COPY_STREAMS
   std::shared_ptr<DevPool> pool;  // device buffers of the handle's factor objects
   GrowBuf batch_ws;               // launch tables of the batched solvers
   GrowBuf solve_ws;               // panels and vectors of ooc_dpotrs_L
@@ -157,6 +159,7 @@ extern "C" int ooc_create(ooc_handle** out, int device) {
   // (oocquark.cpp:260).
   if (cudaStreamCreateWithPriority(&h->s_h2d, cudaStreamNonBlocking, hi) != cudaSuccess ||
       cudaStreamCreateWithPriority(&h->s_d2h, cudaStreamNonBlocking, hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&h->s_h2d2, cudaStreamNonBlocking, hi) != cudaSuccess ||
       cudaStreamCreateWithPriority(&h->s_comp, cudaStreamNonBlocking, lo) != cudaSuccess ||
       cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_wait, cudaEventDisableTiming) != cudaSuccess ||
@@ -187,6 +190,7 @@ extern "C" int ooc_destroy(ooc_handle* h) {
     if (h->s_h2d) cudaStreamSynchronize(h->s_h2d);
     if (h->s_comp) cudaStreamSynchronize(h->s_comp);
     if (h->s_d2h) cudaStreamSynchronize(h->s_d2h);
+    if (h->s_h2d2) cudaStreamSynchronize(h->s_h2d2);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
     if (h->ev_wait) cudaEventDestroy(h->ev_wait);
@@ -198,6 +202,7 @@ extern "C" int ooc_destroy(ooc_handle* h) {
     if (h->s_h2d) cudaStreamDestroy(h->s_h2d);
     if (h->s_comp) cudaStreamDestroy(h->s_comp);
     if (h->s_d2h) cudaStreamDestroy(h->s_d2h);
+    if (h->s_h2d2) cudaStreamDestroy(h->s_h2d2);
   }
   delete h;
   return OOC_OK;
@@ -230,6 +235,10 @@ extern "C" int ooc_set_option(ooc_handle* h, int key, int64_t v) {
       if (v < -1) return -3;
       h->block_cols = v;
       return OOC_OK;
+    case OOC_OPT_COPY_STREAMS:
+      if (v < 1 || v > 2) return -3;
+      h->copy_streams = (int)v;
+      return OOC_OK;
     default: return -2;
   }
 }
@@ -247,6 +256,7 @@ extern "C" int ooc_get_option(ooc_handle* h, int key, int64_t* v) {
     case OOC_OPT_TAIL_ORDER: *v = h->tail_order; return OOC_OK;
     case OOC_OPT_POOL_BYTES: *v = h->pool ? (int64_t)h->pool->cap : 0; return OOC_OK;
     case OOC_OPT_BLOCK_COLS: *v = h->block_cols; return OOC_OK;
+    case OOC_OPT_COPY_STREAMS: *v = h->copy_streams; return OOC_OK;
     default: return -2;
   }
 }
@@ -260,6 +270,7 @@ extern "C" int ooc_get_stream(ooc_handle* h, int which, void** stream) {
     case 0: *stream = (void*)h->s_comp; return OOC_OK;
     case 1: *stream = (void*)h->s_h2d; return OOC_OK;
     case 2: *stream = (void*)h->s_d2h; return OOC_OK;
+    case 3: *stream = (void*)h->s_h2d2; return OOC_OK;
     default: return -2;
   }
 }
