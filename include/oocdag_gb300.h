@@ -90,9 +90,10 @@ enum {
                               = 4096 for device and page-locked host matrices with
                               n > 8192, 0 otherwise.  Needs a plane store of 4 n^2
                               device bytes while the factor is computed.              */
-  OOC_OPT_COPY_STREAMS = 10 /* host-to-device streams a streamed host matrix's column
-                              chunks alternate over (1 or 2; default 1); two keep two
-                              copy engines in flight                                 */
+  OOC_OPT_COPY_STREAMS = 10 /* host-to-device streams that a host matrix streamed into a
+                              split-BF16 factor with a kept copy alternates its column
+                              chunks over (1 or 2; default 2): two copy engines in
+                              flight on the group of columns needed next             */
 };
 
 /* Handles: one per thread of control; reentrant across handles. */

@@ -2267,7 +2267,7 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
   // matrix, or the kept copy once its last chunk has arrived), or chunk by chunk through
   // the staging slots
   std::vector<int> group_of(bb, -1);
-  std::vector<cudaEvent_t> evConv, evCopy2;
+  std::vector<cudaEvent_t> evConv, evCopy1, evCopy2;
   if (side) {
     OOC_CUDA_TRY(cudaStreamWaitEvent(sc2, evP, 0));
     std::vector<std::pair<int, int>> groups{{0, 0}};
@@ -2276,11 +2276,12 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
       if (q1 >= bk.first + 1) groups.emplace_back(bk.first + 1, q1);
     }
     evConv.resize(groups.size());
+    evCopy1.resize(groups.size());
     evCopy2.resize(groups.size());
     for (size_t g = 0; g < groups.size(); g++) {
       const int q0 = groups[g].first, q1 = groups[g].second;
       for (int q = q0; q <= q1; q++) group_of[q] = (int)g;
-      if ((rc = new_event(&evConv[g])) || (rc = new_event(&evCopy2[g]))) return rc;
+      if ((rc = new_event(&evConv[g])) || (rc = new_event(&evCopy1[g])) || (rc = new_event(&evCopy2[g]))) return rc;
       if (!src.on_device) {  // this group's chunks into the kept FP64 copy, in column order,
                              // alternately on the two copy streams (two copy engines in flight)
         if (prof->on && g == 0) {
@@ -2288,6 +2289,10 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
           OOC_CUDA_TRY(cudaEventRecord(prof->h2d0, sc));
           OOC_CUDA_TRY(cudaStreamWaitEvent(sc2, prof->h2d0, 0));
         }
+        // the second stream starts a group only when the first has issued the previous
+        // group's copies: both engines then work on the group the compute stream needs
+        // next, instead of the second racing ahead on later groups and sharing the link
+        if (g > 0 && sc2 != sc) OOC_CUDA_TRY(cudaStreamWaitEvent(sc2, evCopy1[g - 1], 0));
         for (int k = panel_chunks[q0].first; k < panel_chunks[q1].second; k++) {
           const Chunk& c = chunks[k];
           OOC_CUDA_TRY(cudaMemcpy2DAsync(src.keep + c.c0 + c.c0 * n, n * sizeof(double), src.A + c.c0 + c.c0 * src.lda,
@@ -2295,6 +2300,7 @@ int factor_f32_lb(ooc_factor* F, cudaStream_t s0, cudaStream_t s1, cudaStream_t 
                                          cudaMemcpyHostToDevice, (k & 1) ? sc2 : sc));
           prof->h2d_bytes += (double)(n - c.c0) * (double)(c.c1 - c.c0) * sizeof(double);
         }
+        OOC_CUDA_TRY(cudaEventRecord(evCopy1[g], sc));
         OOC_CUDA_TRY(cudaEventRecord(evCopy2[g], sc2));  // sc converts after both streams' copies
         OOC_CUDA_TRY(cudaStreamWaitEvent(sc, evCopy2[g], 0));
         if (prof->on && panel_chunks[q1].second == nchunks) {

@@ -72,7 +72,7 @@ struct ooc_handle {
   int keep_a = 0;
   int64_t tail_order = 24576;
   int64_t block_cols = -1;  // OOC_OPT_BLOCK_COLS (-1: by input)
-  int copy_streams = 1;      // OOC_OPT_COPY_STREAMS
+  int copy_streams = 2;      // OOC_OPT_COPY_STREAMS
   std::shared_ptr<DevPool> pool;  // device buffers of the handle's factor objects
   GrowBuf batch_ws;               // launch tables of the batched solvers
   GrowBuf solve_ws;               // panels and vectors of ooc_dpotrs_L
