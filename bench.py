@@ -46,7 +46,10 @@ METRIC = "Cholesky TFLOP/s (n^3/3 flops), mixed vs FP64 at backward err<=1e-14; 
 # 44.02 GFLOP).  The kernel's traffic is the operand and C tiles, which scale with the
 # flops of a launch at fixed nb.
 UPDATE_DRAM_BYTES_PER_FLOP = 348.1e6 / 44.02e9
-UPDATE_TRAFFIC_RATIO = 967.5 / 976.3  # k_syrk2_bf16x3 bulk launch, n=16384: ncu DRAM bytes / algorithmic bytes
+# ncu DRAM bytes / algorithmic bytes of one long-K catch-up launch (k_syrk2t_bf16x3, n=16384,
+# m=12032, 3840 columns, K=4096: 698.1 + 140.1 MB measured against 8 B per lower element of
+# C plus 4 B per plane element, 507.8 MB); the catch-ups carry 90 % of the update flops
+UPDATE_TRAFFIC_RATIO = (698.1 + 140.1) / 507.8
 
 
 def parse():
@@ -733,8 +736,9 @@ def run_mixed(args):
     share_fac = fac_ms / (ms_local * args.steps)
     bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
     mult = 3 if args.prec == "bf16x3" else 1
-    upd_roof = {"kernel": "k_syrk2_bf16x3<float> (persistent split-BF16 tcgen05 trailing update, 256x128 blocks, "
-                          "FP32 C updated by TMA reductions)"
+    upd_roof = {"kernel": "k_syrk2t_bf16x3 (long-K catch-ups: N=256 tcgen05 MMAs, C transposed in TMEM, four-stage "
+                          "K=32 operand ring) + k_syrk2_bf16x3<float> (in-block K=256 updates): persistent split-BF16 "
+                          "trailing updates, 256x128 blocks, FP32 C updated by TMA reductions"
                 if args.prec == "bf16x3" else "k_syrk_f32<float> (FP32 FFMA trailing update)",
                 "bound": "tensor" if args.prec == "bf16x3" else "fp32-simt",
                 "achieved": upd_flops / (upd_ms / 1e3) / 1e12 if upd_ms else None,
@@ -756,12 +760,11 @@ def run_mixed(args):
         upd_roof["tensor_pipe_frac"] = upd_roof["tensor_pipe_achieved"] / upd_roof["peak"]
     if args.prec == "bf16x3" and upd_launch:
         # DRAM bytes per launch: the algorithmic kernel bytes scaled by the measured/algorithmic
-        # ratio of one ncu capture (bulk update at n=16384 with 512-wide panels, m=15872, block columns 4..:
-        # 967.5 MB measured, 976.3 MB algorithmic)
+        # ratio of one ncu capture (UPDATE_TRAFFIC_RATIO: a long-K catch-up launch at n=16384)
         upd_roof["traffic"] = UPDATE_TRAFFIC_RATIO * kern_bytes / upd_launch
-        upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per algorithmic byte of "
-                                      "update launches captured at n=16384 (profiles/), times this workload's "
-                                      "algorithmic bytes per launch")
+        upd_roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per algorithmic byte of a "
+                                      "long-K catch-up launch captured at n=16384 (profiles/), times this "
+                                      "workload's algorithmic bytes per launch")
         upd_roof["schedule"] = sched["kind"]
     chain_flops = sum(2 * LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in panels) * args.steps
     fac_roof = {"kernel": "diagonal chain: k_diag_s256 / k_diag_f32 (FP32 potrf + inverse of the 256- / 512-wide "
