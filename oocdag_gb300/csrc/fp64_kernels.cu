@@ -42,65 +42,72 @@ __device__ __forceinline__ void dmma884(double& c0, double& c1, double a, double
                : "d"(a), "d"(b));
 }
 
-// Loads rows [r0, r0+64) x columns [k0, k0+16) of the column-major operand M (rows
-// valid below `rows`, columns below `kmax`) into S[k][r] (row length LDS).
-template <bool VEC>
+// Loads rows [r0, r0+BMX) x columns [k0, k0+16) of the column-major operand M (rows
+// valid below `rows`, columns below `kmax`) into S[k][r] (row length BMX + PAD).
+template <bool VEC, int BMX = BM>
 __device__ __forceinline__ void load_slab(double* S, const double* M, i64 ld, int r0, int rows,
                                           int k0, int kmax) {
+  constexpr int L = BMX + PAD;
   const int t = threadIdx.x;
   if (VEC) {
 #pragma unroll
-    for (int it = 0; it < (BM * BK / 2) / GEMM_THREADS; it++) {
+    for (int it = 0; it < (BMX * BK / 2) / GEMM_THREADS; it++) {
       int idx = t + it * GEMM_THREADS;
-      int kc = idx / (BM / 2);
-      int r = (idx % (BM / 2)) * 2;
+      int kc = idx / (BMX / 2);
+      int r = (idx % (BMX / 2)) * 2;
       int gr = r0 + r, gk = k0 + kc;
       int nvalid = 0;
       if (gk < kmax) nvalid = min(max(rows - gr, 0), 2);
       const double* src = (nvalid > 0) ? (M + gr + (i64)gk * ld) : M;
-      cp_async16(S + kc * LDS + r, src, nvalid * 8);
+      cp_async16(S + kc * L + r, src, nvalid * 8);
     }
   } else {
-    for (int idx = t; idx < BM * BK; idx += GEMM_THREADS) {
-      int kc = idx / BM;
-      int r = idx % BM;
+    for (int idx = t; idx < BMX * BK; idx += GEMM_THREADS) {
+      int kc = idx / BMX;
+      int r = idx % BMX;
       int gr = r0 + r, gk = k0 + kc;
-      S[kc * LDS + r] = (gr < rows && gk < kmax) ? M[gr + (i64)gk * ld] : 0.0;
+      S[kc * L + r] = (gr < rows && gk < kmax) ? M[gr + (i64)gk * ld] : 0.0;
     }
   }
 }
 
-// C[m0:m0+64, n0:n0+64] += alpha * A[m0:, 0:k] * B[n0:, 0:k]^T, restricted to the lower
-// triangle (row >= column) when `lower` is set.
-template <bool VEC>
+// C[m0:m0+BMX, n0:n0+BMX] += alpha * A[m0:, 0:k] * B[n0:, 0:k]^T, restricted to the lower
+// triangle (row >= column) when `lower` is set.  Four warps in a 2 x 2 arrangement, each
+// (BMX/2) x (BMX/2) as (BMX/16)^2 DMMA tiles.  BMX = 32 gives four times as many CTAs for
+// the same output (for launches too small to fill the GPU with 64 x 64 blocks); every
+// output element takes the same DMMA steps in the same order either way.
+template <bool VEC, int BMX = BM>
 __device__ __forceinline__ void gemm_block(const double* __restrict__ A, i64 lda,
                                            const double* __restrict__ B, i64 ldb,
                                            double* __restrict__ C, i64 ldc, int m, int n, int k,
                                            int m0, int n0, int lower, double alpha) {
-  __shared__ __align__(16) double As[2][BK * LDS];
-  __shared__ __align__(16) double Bs[2][BK * LDS];
+  constexpr int L = BMX + PAD;
+  constexpr int TI = BMX / 16;  // DMMA tiles per warp dimension
+  constexpr int WT = BMX / 2;   // warp tile
+  __shared__ __align__(16) double As[2][BK * L];
+  __shared__ __align__(16) double Bs[2][BK * L];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wm = warp & 1, wn = warp >> 1;
   const int g = lane >> 2, tig = lane & 3;
 
-  double acc[4][4][2];
+  double acc[TI][TI][2];
 #pragma unroll
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < TI; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
+    for (int j = 0; j < TI; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
 
   const int nslab = (k + BK - 1) / BK;
   if (nslab > 0) {
-    load_slab<VEC>(As[0], A, lda, m0, m, 0, k);
-    load_slab<VEC>(Bs[0], B, ldb, n0, n, 0, k);
+    load_slab<VEC, BMX>(As[0], A, lda, m0, m, 0, k);
+    load_slab<VEC, BMX>(Bs[0], B, ldb, n0, n, 0, k);
     if (VEC) cp_async_commit();
   }
   for (int s = 0; s < nslab; s++) {
     const int cur = s & 1;
     if (s + 1 < nslab) {
-      load_slab<VEC>(As[cur ^ 1], A, lda, m0, m, (s + 1) * BK, k);
-      load_slab<VEC>(Bs[cur ^ 1], B, ldb, n0, n, (s + 1) * BK, k);
+      load_slab<VEC, BMX>(As[cur ^ 1], A, lda, m0, m, (s + 1) * BK, k);
+      load_slab<VEC, BMX>(Bs[cur ^ 1], B, ldb, n0, n, (s + 1) * BK, k);
       if (VEC) { cp_async_commit(); cp_async_wait<1>(); }
     } else {
       if (VEC) cp_async_wait<0>();
@@ -110,15 +117,15 @@ __device__ __forceinline__ void gemm_block(const double* __restrict__ A, i64 lda
     const double* bs = Bs[cur];
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 4) {
-      double a[4], b[4];
+      double a[TI], b[TI];
 #pragma unroll
-      for (int i = 0; i < 4; i++) a[i] = as[(kk + tig) * LDS + wm * 32 + i * 8 + g];
+      for (int i = 0; i < TI; i++) a[i] = as[(kk + tig) * L + wm * WT + i * 8 + g];
 #pragma unroll
-      for (int j = 0; j < 4; j++) b[j] = bs[(kk + tig) * LDS + wn * 32 + j * 8 + g];
+      for (int j = 0; j < TI; j++) b[j] = bs[(kk + tig) * L + wn * WT + j * 8 + g];
 #pragma unroll
-      for (int i = 0; i < 4; i++)
+      for (int i = 0; i < TI; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) dmma884(acc[i][j][0], acc[i][j][1], a[i], b[j]);
+        for (int j = 0; j < TI; j++) dmma884(acc[i][j][0], acc[i][j][1], a[i], b[j]);
     }
     __syncthreads();
   }
@@ -126,22 +133,22 @@ __device__ __forceinline__ void gemm_block(const double* __restrict__ A, i64 lda
   // Epilogue, one 8-row group at a time: its loads of C first, then its stores (a load
   // after a store to a possibly aliasing address would wait for memory each time).
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int r = m0 + wm * 32 + i * 8 + g;
-    double cv[4][2];
+  for (int i = 0; i < TI; i++) {
+    const int r = m0 + wm * WT + i * 8 + g;
+    double cv[TI][2];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int j = 0; j < TI; j++)
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        const int c = n0 + wn * 32 + j * 8 + 2 * tig + h;
+        const int c = n0 + wn * WT + j * 8 + 2 * tig + h;
         const bool ok = r < m && c < n && !(lower && c > r);
         cv[j][h] = ok ? C[r + (i64)c * ldc] : 0.0;
       }
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int j = 0; j < TI; j++)
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        const int c = n0 + wn * 32 + j * 8 + 2 * tig + h;
+        const int c = n0 + wn * WT + j * 8 + 2 * tig + h;
         if (r < m && c < n && !(lower && c > r)) C[r + (i64)c * ldc] = fma(alpha, acc[i][j][h], cv[j][h]);
       }
   }
@@ -188,19 +195,19 @@ struct GemmBatch {
   int tri_b;  // B lower triangular (B(j, kk) = 0 for kk > j): skip the zero K range
 };
 
-template <bool VEC>
+template <bool VEC, int BMX = BM>
 __global__ void __launch_bounds__(GEMM_THREADS) k_gemm_batched(GemmBatch gb, const int* status) {
   if (status && *(volatile const int*)status) return;
   const int z = blockIdx.y;
   const int m = (z == gb.batch - 1) ? gb.m_last : gb.m;
-  const int mblocks = (max(gb.m, gb.m_last) + BM - 1) / BM;
-  const int m0 = (blockIdx.x % mblocks) * BM;
-  const int n0 = (blockIdx.x / mblocks) * BN;
+  const int mblocks = (max(gb.m, gb.m_last) + BMX - 1) / BMX;
+  const int m0 = (blockIdx.x % mblocks) * BMX;
+  const int n0 = (blockIdx.x / mblocks) * BMX;
   if (m0 >= m || n0 >= gb.n) return;
-  if (gb.lower && n0 > m0 + BM - 1) return;
-  const int kmax = gb.tri_b ? min(gb.k, n0 + BN) : gb.k;
-  gemm_block<VEC>(gb.A + (i64)z * gb.sA, gb.lda, gb.B + (i64)z * gb.sB, gb.ldb,
-                  gb.C + (i64)z * gb.sC, gb.ldc, m, gb.n, kmax, m0, n0, gb.lower, gb.alpha);
+  if (gb.lower && n0 > m0 + BMX - 1) return;
+  const int kmax = gb.tri_b ? min(gb.k, n0 + BMX) : gb.k;
+  gemm_block<VEC, BMX>(gb.A + (i64)z * gb.sA, gb.lda, gb.B + (i64)z * gb.sB, gb.ldb,
+                       gb.C + (i64)z * gb.sC, gb.ldc, m, gb.n, kmax, m0, n0, gb.lower, gb.alpha);
 }
 
 // ---------------------------------------------------------------------------------
@@ -377,8 +384,24 @@ static int launch_gemm_batched(const GemmBatch& gb, const int* status, cudaStrea
   bool vec = aligned16(gb.A) && aligned16(gb.B) && aligned16(gb.C) && gb.lda % 2 == 0 &&
              gb.ldb % 2 == 0 && gb.sA % 2 == 0 && gb.sB % 2 == 0;
   if (gb.k <= 0) return OOC_OK;
-  if (vec) k_gemm_batched<true><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
-  else k_gemm_batched<false><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
+  // Fewer 64 x 64 blocks than two per SM: 32 x 32 blocks, four times as many CTAs (the
+  // FP64 pipe of an SM does ~2 FMAs per clock, so a 64 x 64 x 64 block alone takes ~75 us)
+  static int nsm = [] {
+    int d = 0, v = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d);
+    return v > 0 ? v : 1;
+  }();
+  if ((i64)mb * nbk * gb.batch < 2LL * nsm && (i64)gb.batch <= 65535) {
+    const int mb32 = (max(gb.m, gb.m_last) + 31) / 32, nb32 = (gb.n + 31) / 32;
+    dim3 g32(mb32 * nb32, gb.batch);
+    if (vec) k_gemm_batched<true, 32><<<g32, GEMM_THREADS, 0, s>>>(gb, status);
+    else k_gemm_batched<false, 32><<<g32, GEMM_THREADS, 0, s>>>(gb, status);
+  } else if (vec) {
+    k_gemm_batched<true><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
+  } else {
+    k_gemm_batched<false><<<grid, GEMM_THREADS, 0, s>>>(gb, status);
+  }
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }
