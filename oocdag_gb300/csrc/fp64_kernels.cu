@@ -267,88 +267,75 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
 
 // ---------------------------------------------------------------------------------
 // B := B L^-T for a block of up to 64 columns: L is n x n lower (n <= 64), B rows are
-// independent.  One thread per row, TS_ROWS rows per CTA (small CTAs spread a short
-// panel over more SMs: FP64 issues at ~2 FMAs per clock per SM); z = blockIdx.y walks a
-// batch of row panels (tiles) with stride sB, the last of which has m_last rows.
-// Right-looking inside the row: once x_c is final, every later column takes its FMA with
-// it, so a row's 2016 FMAs are independent across columns instead of one dependent chain
-// per column; each column still receives its updates in increasing q.  The row is done
-// in two halves of 32 columns held in registers; the first half's results wait in shared
-// memory while they update the second.  L sits in shared memory, padded to 64 with the
-// identity, and is read by broadcast; x_c = v * (1 / L(c,c)).
+// independent.  Four lanes per row, each holding every fourth column in registers, 32 rows
+// per CTA of 128 threads; z = blockIdx.y walks a batch of row panels (tiles) with stride
+// sB, the last of which has m_last rows.  FP64 issues from each SM sub-partition at about
+// one FMA per two clocks, so a row group must spread over the sub-partitions: one thread
+// per row left three of them idle and took ~100 us per 64-column step.  Right-looking:
+// once x_c is final (computed by its owner lane and passed to the row's other lanes by a
+// shuffle), every later column takes its FMA with it, in increasing c, as a substitution
+// does.  L sits in shared memory, padded to 64 with the identity, and is read by broadcast;
+// x_c = v * (1 / L(c,c)).
 // ---------------------------------------------------------------------------------
-constexpr int TS_ROWS = 32;
-constexpr int TS_H = SB / 2;
+constexpr int TS_ROWS = 32;                  // rows per CTA
+constexpr int TS_LPR = 4;                    // lanes per row
+constexpr int TS_THREADS = TS_ROWS * TS_LPR;
+constexpr int TS_C = SB / TS_LPR;            // columns per lane
 
-// x[0..TS_H) := x L(c0.., c0..)^-T for the 32 columns starting at c0, right-looking.
-// `zero` is 0 at run time; adding (zero & bits of x_c) to the address makes column c's
-// loads of L wait for x_c, so the compiler does not hoist all 496 loads into registers.
-__device__ __forceinline__ void trsm_half(double (&x)[TS_H], const double* Ls, const double* Rinv, int c0,
-                                          int zero) {
-#pragma unroll
-  for (int c = 0; c < TS_H; c++) {
-    x[c] *= Rinv[c0 + c];
-    const double* lc = Ls + (c0 + c) * SB + c0 + (zero & __double2hiint(x[c]));
-#pragma unroll
-    for (int q = c + 1; q < TS_H; q++) x[q] = fma(-x[c], lc[q], x[q]);
-  }
-}
-
-__global__ void __launch_bounds__(TS_ROWS) k_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB,
-                                                        int m, int m_last, int batch, int n,
-                                                        const int* status) {
+__global__ void __launch_bounds__(TS_THREADS) k_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 sB,
+                                                           int m, int m_last, int batch, int n,
+                                                           const int* status) {
   if (status && *(volatile const int*)status) return;
   __shared__ __align__(16) double Ls[SB * SB];  // Ls[c * SB + r] = L(r, c)
   __shared__ double Rinv[SB];
-  __shared__ double Xs[TS_H * TS_ROWS];         // first half's results, Xs[c * TS_ROWS + t]
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31;
+  const int s = t & (TS_LPR - 1);   // this lane holds columns s, s + 4, ...
   const int z = blockIdx.y;
   const int mz = (z == batch - 1) ? m_last : m;
   const int r0 = blockIdx.x * TS_ROWS;
   if (r0 >= mz) return;
   double* Bz = B + (i64)z * sB;
-  // L column by column, lanes down the rows: 16 loads in flight per thread (one warp
-  // cannot hide a load's latency one element at a time)
+  {  // L column by column, threads down the rows (two columns per pass), 8 loads in flight
+    const int r = t & (SB - 1), cg = t / SB;
 #pragma unroll 8
-  for (int c = 0; c < SB; c++) {
-#pragma unroll
-    for (int h = 0; h < SB / TS_ROWS; h++) {
-      const int r = t + TS_ROWS * h;
+    for (int c = cg; c < SB; c += TS_THREADS / SB) {
       double v = (r == c) ? 1.0 : 0.0;
       if (r < n && c < n && r >= c) v = L[r + (i64)c * ldl];
       Ls[c * SB + r] = v;
     }
   }
   __syncthreads();
-  for (int c = t; c < SB; c += TS_ROWS) Rinv[c] = 1.0 / Ls[c * SB + c];
-  const int row = r0 + t;
-  const int nl = (row < mz) ? n : 0;  // columns this thread loads and stores
+  if (t < SB) Rinv[t] = 1.0 / Ls[t * SB + t];
+  const int row = r0 + t / TS_LPR;
+  const int nl = (row < mz) ? n : 0;  // columns this row loads and stores
   double* p = Bz + (row < mz ? row : 0);
-  double x[TS_H];
+  double x[TS_C];
 #pragma unroll
-  for (int c = 0; c < TS_H; c++) x[c] = (c < nl) ? p[(i64)c * ldb] : 0.0;
+  for (int j = 0; j < TS_C; j++) {
+    const int q = TS_LPR * j + s;
+    x[j] = (q < nl) ? p[(i64)q * ldb] : 0.0;
+  }
   __syncthreads();
-  const int zero = n >> 30;  // n <= 64
-  trsm_half(x, Ls, Rinv, 0, zero);
+  const int zero = n >> 30;  // n <= 64: 0 at run time, opaque to the compiler
+  const int base = lane & ~(TS_LPR - 1);
 #pragma unroll
-  for (int c = 0; c < TS_H; c++) {
-    Xs[c * TS_ROWS + t] = x[c];
-    if (c < nl) p[(i64)c * ldb] = x[c];
+  for (int c = 0; c < SB; c++) {
+    const int i = c / TS_LPR, sc = c % TS_LPR;
+    const double xc = __shfl_sync(0xffffffffu, x[i] * Rinv[c], base | sc);  // the owner's x_c
+    if (s == sc) x[i] = xc;
+    // column c's loads of L wait for x_c (not all hoisted into registers)
+    const double* lc = Ls + c * SB + (zero & __double2hiint(xc));
+#pragma unroll
+    for (int j = 0; j < TS_C; j++) {
+      const int q = TS_LPR * j + s;
+      if (q > c) x[j] = fma(-xc, lc[q], x[j]);
+    }
   }
-  if (n <= TS_H) return;
 #pragma unroll
-  for (int c = 0; c < TS_H; c++) x[c] = (TS_H + c < nl) ? p[(i64)(TS_H + c) * ldb] : 0.0;
-  // the second half's updates from the first half, in increasing c
-  for (int c = 0; c < TS_H; c++) {
-    const double xc = Xs[c * TS_ROWS + t];
-    const double* lc = Ls + c * SB + TS_H + (zero & __double2hiint(xc));
-#pragma unroll
-    for (int q = 0; q < TS_H; q++) x[q] = fma(-xc, lc[q], x[q]);
+  for (int j = 0; j < TS_C; j++) {
+    const int q = TS_LPR * j + s;
+    if (q < nl) p[(i64)q * ldb] = x[j];
   }
-  trsm_half(x, Ls, Rinv, TS_H, zero);
-#pragma unroll
-  for (int c = 0; c < TS_H; c++)
-    if (TS_H + c < nl) p[(i64)(TS_H + c) * ldb] = x[c];
 }
 
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
@@ -423,7 +410,7 @@ static int launch_trsm_small(const double* L, i64 ldl, double* B, i64 ldb, i64 s
   if (batch <= 0 || n <= 0) return OOC_OK;
   if (n > SB) return OOC_ERR_INTERNAL;
   dim3 grid((max(m, m_last) + TS_ROWS - 1) / TS_ROWS, batch);
-  k_trsm_small<<<grid, TS_ROWS, 0, s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
+  k_trsm_small<<<grid, TS_THREADS, 0, s>>>(L, ldl, B, ldb, sB, m, m_last, batch, n, status);
   OOC_CUDA_TRY(cudaGetLastError());
   return OOC_OK;
 }
