@@ -364,6 +364,38 @@ def test_left_looking_blocks(oracle_mod, handle, ooc, where, keep, nb, bcols, n)
     assert _berr(A, _host(Xd), B) <= 2 * BERR_TOL
 
 
+def test_copy_streams_do_not_change_the_factor(oracle_mod, handle, ooc):
+    # A page-locked host matrix streamed into the left-looking factor over one or two
+    # host-to-device streams (OOC_OPT_COPY_STREAMS): the copies only move bytes, so the
+    # factors are identical bit for bit, and both refine to the FP64 bar.
+    import torch
+
+    n, nb = 9000, 512
+    A, _ = _c2_matrix(oracle_mod, n, 0.1)
+    Ah = torch.from_numpy(np.ascontiguousarray(A.T)).pin_memory()
+    B = np.asfortranarray(np.random.default_rng(4).standard_normal((n, 1)))
+    Ls = []
+    handle.set_option(ooc.OPT_KEEP_A, 1)
+    handle.set_option(ooc.OPT_BLOCK_COLS, 2048)
+    try:
+        for cs in (1, 2):
+            handle.set_option(ooc.OPT_COPY_STREAMS, cs)
+            assert handle.get_option(ooc.OPT_COPY_STREAMS) == cs
+            L = np.asfortranarray(np.full((n, n), np.nan))
+            Bd, Xd = _dev(B), _dev(np.zeros((n, 1)))
+            with handle.factor(Ah, n, n, nb, "bf16x3") as F:
+                assert F.info == 0
+                F.copy_L(L, n)
+                it, be = F.refine(Ah, n, Bd, n, Xd, n, 1, BERR_TOL, 30)
+            assert be <= BERR_TOL and it <= 5, (cs, it, be)
+            Ls.append(L)
+    finally:
+        handle.set_option(ooc.OPT_COPY_STREAMS, 2)
+        handle.set_option(ooc.OPT_BLOCK_COLS, -1)
+        handle.set_option(ooc.OPT_KEEP_A, 0)
+    np.testing.assert_array_equal(Ls[0], Ls[1])
+
+
 def test_left_looking_blocks_report_lapack_info(oracle_mod, handle, ooc):
     import torch
 
