@@ -250,10 +250,15 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
     const double inv = s_inv;
     for (int r = j + 1 + t; r < n; r += blockDim.x) S[j][r] *= inv;
     __syncthreads();
-    const int w = n - j - 1;  // trailing (w x w) lower triangle
-    for (int idx = t; idx < w * w; idx += blockDim.x) {
-      int c = j + 1 + idx / w, r = j + 1 + idx % w;
-      if (r >= c) S[c][r] -= S[j][r] * S[j][c];
+    // trailing lower triangle: thread t takes row j + 1 + (t mod 64) and every fourth
+    // column from j + 1 + (t / 64) up to that row (independent updates, no index division)
+    {
+      const int r = j + 1 + (t & (SB - 1));
+      if (r < n) {
+        const double lr = S[j][r];
+#pragma unroll 4
+        for (int c = j + 1 + (t >> 6); c <= r; c += 4) S[c][r] -= lr * S[j][c];
+      }
     }
     __syncthreads();
   }
