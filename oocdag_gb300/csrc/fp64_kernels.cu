@@ -25,7 +25,6 @@ constexpr int BM = 64;
 constexpr int BN = 64;
 constexpr int BK = 16;
 constexpr int PAD = 4;               // row length BM+PAD makes fragment loads conflict-free
-constexpr int LDS = BM + PAD;        // shared row length (doubles)
 constexpr int GEMM_THREADS = 128;    // 4 warps in a 2 x 2 arrangement, 32 x 32 each
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
@@ -231,23 +230,30 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
       if (r < n && c < n && r >= c) S[c][r] = A[r + (i64)c * ld];
     }
   }
-  if (t == 0) failed = 0;
+  // Column j's pivot (one FP64 square root and one division, by thread 0).  Thread 0 also
+  // owns element (j+1, j+1) in column j's trailing update (row j + 1 + 0, first column
+  // group), so it takes the next pivot as soon as that element is final, while the other
+  // threads are still updating: two barriers per column, and the serial pivot mostly off
+  // the barrier-to-barrier path.
+  auto pivot = [&](int j) {
+    const double d = S[j][j];
+    if (!(d > 0.0)) {
+      failed = 1;
+      atomicCAS(status, 0, (int)(col0 + j + 1));
+    } else {
+      const double sq = sqrt(d);
+      S[j][j] = sq;
+      s_inv = 1.0 / sq;
+    }
+  };
+  if (t == 0) {
+    failed = 0;
+    if (n > 0) pivot(0);
+  }
   __syncthreads();
   for (int j = 0; j < n; j++) {
-    if (t == 0) {  // one FP64 square root and one division per column, not one per thread
-      double d = S[j][j];
-      if (!(d > 0.0)) {
-        failed = 1;
-        atomicCAS(status, 0, (int)(col0 + j + 1));
-      } else {
-        const double sq = sqrt(d);
-        S[j][j] = sq;
-        s_inv = 1.0 / sq;
-      }
-    }
-    __syncthreads();
     if (failed) break;
-    const double inv = s_inv;
+    const double inv = s_inv;  // read before the barrier below; thread 0 rewrites it after
     for (int r = j + 1 + t; r < n; r += blockDim.x) S[j][r] *= inv;
     __syncthreads();
     // trailing lower triangle: thread t takes row j + 1 + (t mod 64) and every fourth
@@ -260,6 +266,7 @@ __global__ void __launch_bounds__(256) k_potrf_small(double* A, i64 ld, int n, i
         for (int c = j + 1 + (t >> 6); c <= r; c += 4) S[c][r] -= lr * S[j][c];
       }
     }
+    if (t == 0 && j + 1 < n) pivot(j + 1);
     __syncthreads();
   }
   // Columns factored before a failure are written back as well (LAPACK leaves the
