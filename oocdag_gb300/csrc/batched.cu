@@ -1,14 +1,18 @@
 // Batched factor + solve of many small SPD systems in ONE persistent launch.
 //
 // Thousands of uneven matrices (n in [16, 512]) are too small for the tile pipeline:
-// each would be a handful of tiny launches.  Here every CTA of a persistent grid takes
-// the next matrix from a queue sorted by decreasing size (largest first balances the
-// tail), factors it with a blocked right-looking Cholesky inside the CTA (diagonal block
-// in shared memory, factored by one warp in registers for FP32 and column by column by
-// the CTA for FP64; panel solve thread-per-row with the row in registers; trailing update
-// from a shared-memory copy of the panel with 4 x 4 register tiles), then solves for its
-// right-hand side, and moves on.  Per-matrix LAPACK info goes to an array; a failed matrix is skipped.
-// The panel width is chosen per size bucket by the autotuner (oocdag_gb300/autotune.py).
+// each would be a handful of tiny launches.  Here every CTA of a persistent grid (one
+// launch per size class) takes the next matrix from a queue sorted by decreasing size
+// (largest first balances the tail), factors it with a blocked right-looking Cholesky
+// inside the CTA, solves for its right-hand side, and moves on.  FP32 (factor_f32): the
+// diagonal block factored by one warp in registers, the panel solved a row per thread in
+// registers and kept transposed in shared memory, the trailing update by 32 x 32 blocks
+// with a 4 x 8 register tile per lane, the forward substitution inside the factorization
+// and the backward sweep on the vector in shared memory.  FP64 (factor_one): the diagonal
+// block column by column by the CTA, the panel solve a row per thread, the trailing update
+// from a row copy of the panel with 4 x 4 register tiles, then both sweeps (solve_one).
+// Per-matrix LAPACK info goes to an array; a failed matrix is skipped.  The panel width is
+// chosen per size bucket by the autotuner (oocdag_gb300/autotune.py).
 //
 // The per-tile arithmetic restates the reference's task bodies at small n: the
 // diagonal dpotrf (oocquark.cpp:87), the column dtrsm R/L/T/N (:130) and the

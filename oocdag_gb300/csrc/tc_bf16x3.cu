@@ -6,6 +6,9 @@
 //   k_syrk2_bf16x3<TC>  the same for 16-byte-aligned FP32 C (the working matrix of
 //                       reduced-precision factors) in 256 x 128 blocks, C updated by TMA
 //                       reductions, blocks taken from a run-time ticket counter;
+//   k_syrk2t_bf16x3     the same update for long K (the left-looking catch-ups), issued
+//                       as N=256 MMAs with C transposed in TMEM, fed by four 48 KB stages
+//                       of K = 32 (64-byte swizzle);
 //   k_trsm2_bf16x3      the column solve P = U X^T with the same three products.
 // Each kernel's own comment gives its layout; the 128 x 128 update is described here.
 //
