@@ -55,6 +55,25 @@ def test_panel_schedule_default_workload():
 
 
 # ---------------------------------------------------------------- autotuner table
+@pytest.mark.parametrize("n,block_cols", [(65536, -1), (16384, -1), (20000, 2048), (65536, 0)])
+def test_update_schedule_accounts_for_the_cholesky_flops(n, block_cols):
+    # The bench's roofline counts 2 K flops per lower-triangle output element of every
+    # trailing-update launch in the schedule the library runs (left-looking catch-ups and
+    # in-block updates, or right-looking panels).  Together they must be the Cholesky's
+    # n^3/3 less the diagonal tiles' own factor and column-solve work: never more, and
+    # only a small share less.
+    nb = 512
+    s = bench.update_schedule(n, nb, "bf16x3", 24576, block_cols)
+    upd = sum(2 * K * bench.lower_elems(m, c) for m, K, c in s["launches"])
+    total = n ** 3 / 3
+    diag = sum(LN ** 3 / 3 + (n - J0 - LN) * LN * LN for J0, LN in s["panels"])
+    assert upd <= total
+    assert abs(upd + diag - total) <= 0.01 * total, (upd, diag, total)
+    if block_cols != 0:
+        assert s["kind"].startswith("left-looking")
+        assert all(K <= bench.CATCH_K for _, K, _ in s["launches"])
+
+
 def test_autotune_table_round_trip(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "_gpu_name", lambda: "Test GPU")
     path = str(tmp_path / "sub" / "t.json")
