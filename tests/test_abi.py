@@ -105,6 +105,10 @@ def test_every_entry_point_checks_its_handle_first(ooc):
     assert L.ooc_batched_dposv(None, 1, ns, off, off, buf, buf, b(info), None, 0, b(d)) == -1
     assert L.ooc_batched_sposv(None, 1, ns, off, off, buf, buf, b(info), None, 0, b(d)) == -1
     assert L.ooc_get_option(None, ooc.OPT_TAIL_ORDER, b(v)) == -1
+    assert L.ooc_get_option(None, ooc.OPT_COPY_STREAMS, b(v)) == -1
+    assert L.ooc_set_option(None, ooc.OPT_COPY_STREAMS, 2) == -1
+    sp = ctypes.c_void_p()
+    assert L.ooc_get_stream(None, 3, b(sp)) == -1
     assert L.ooc_last_info(None) == 0
     assert L.ooc_destroy(None) == ooc.OOC_OK
     assert L.ooc_dpotrs_L(None, buf, 4, 4, 4, 0, buf, 4, 1) == -1
